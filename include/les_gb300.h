@@ -1,0 +1,210 @@
+/*
+ * les_gb300.h -- C ABI of the GB300 (sm_103a) implementation of the
+ * les-model per-time-step hot path.
+ *
+ * One context owns a device mirror of one reference Field (src/field.h:9-41)
+ * plus the pressure system (StencilMatrix A and IC factor L,
+ * src/pressure.h:17-29) and all solver work vectors, on one GPU and one CUDA
+ * stream.  Every entry point below replaces one reference function; the
+ * comment on each names it (file:line in the les-model sources).  Array
+ * layout is the reference's: idx = i*ny*nz + j*nz + k (src/field.h:40).
+ *
+ * Conventions
+ *  - All functions return an les_status; nothing throws across the ABI.
+ *  - Calls are asynchronous on the context's stream unless they return a
+ *    host scalar (dt, iteration counts, lambda), which synchronise.
+ *  - Host buffers passed in are read before the call returns; host buffers
+ *    passed out are complete when the call returns.
+ *  - One context per host thread; contexts share nothing.
+ */
+#ifndef LES_GB300_H
+#define LES_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LES_ABI_VERSION 1
+
+typedef enum les_status {
+    LES_OK = 0,
+    LES_NOT_CONVERGED = 1, /* iteration cap reached (the reference warns on stderr) */
+    LES_NONFINITE = 2,     /* a residual or scalar became NaN/Inf */
+    LES_BAD_ARG = 3,
+    LES_CUDA_ERROR = 4,    /* les_last_error() has the CUDA message */
+    LES_NO_DEVICE = 5,
+    LES_TIMEOUT = 6        /* a bounded device-side wait gave up */
+} les_status;
+
+/* Mirrors Mesh, src/field.h:6. */
+typedef struct les_mesh {
+    int nx, ny, nz;
+    double dx, dy, dz;
+} les_mesh;
+
+typedef struct les_ctx les_ctx;
+
+/* Device arrays of the reference Field (src/field.h:13-20) plus the PCG
+ * right-hand side b that src/main.cpp:135 allocates every step. */
+typedef enum les_slot {
+    LES_U = 0, LES_V, LES_W, LES_U_NEW, LES_V_NEW, LES_W_NEW,
+    LES_P, LES_P_RHS, LES_NU_T, LES_B,
+    LES_NSLOTS
+} les_slot;
+
+/* Pressure solvers, chosen at run time (the reference selects them by
+ * commenting lines out, src/main.cpp:131-138). */
+typedef enum les_solver {
+    LES_SOLVER_PCG = 0,      /* src/pressure.cpp:342-414 / :762-835 */
+    LES_SOLVER_JACOBI = 1,   /* src/pressure.cpp:106-172 */
+    LES_SOLVER_GS_SOR = 2    /* src/pressure.cpp:186-247 */
+} les_solver;
+
+typedef enum les_precond {
+    LES_PC_JACOBI = 0,     /* apply_jacobi_preconditioner, src/pressure.cpp:420-428 */
+    LES_PC_IC = 1,         /* apply_ic_preconditioner with L from build_ic_preconditioner */
+    LES_PC_CHEBYSHEV = 2,  /* apply_chebyshev_preconditioner, src/pressure.cpp:851-906 */
+    LES_PC_IC_A = 3        /* as shipped: apply_ic_preconditioner(..., A, ...), :363, :396 */
+} les_precond;
+
+typedef enum les_precision {
+    LES_FP64 = 0,   /* the reference's arithmetic */
+    LES_MIXED = 1   /* FP32 inner PCG inside FP64 defect correction */
+} les_precision;
+
+typedef struct les_pcg_opts {
+    int precond;          /* les_precond */
+    int max_iter;         /* FP64: PCG iterations (reference: 1000, src/main.cpp:137);
+                             MIXED: cap on the total inner iterations */
+    double tol;           /* absolute tolerance on ||b - A x||_2 (reference semantics) */
+    double lambda_min, lambda_max; /* Chebyshev bounds */
+    int degree;           /* Chebyshev polynomial degree (reference default 5) */
+    int precision;        /* les_precision */
+    double inner_rtol;    /* MIXED: inner FP32 solve reduces its residual by this */
+    int inner_max_iter;   /* MIXED: cap per inner solve */
+    int max_outer;        /* MIXED: cap on defect-correction sweeps */
+} les_pcg_opts;
+
+typedef struct les_pcg_result {
+    int iters;            /* FP64: reference iteration count; MIXED: total inner iterations */
+    int outer;            /* MIXED: defect-correction sweeps (0 for FP64) */
+    double residual;      /* final ||b - A x||_2 in FP64 */
+} les_pcg_result;
+
+typedef struct les_step_params {
+    double nu, rho, cs;             /* reference: 1e-5, 1.2 (src/main.cpp:83-84), 0.18 (:425) */
+    double cfl_conv, cfl_visc, dt_max; /* reference: 0.4, 0.2, 1e-4 (src/main.cpp:210-212) */
+    double dt_fixed;                /* > 0: use this dt instead of compute_adaptive_dt */
+    int solver;                     /* les_solver */
+    les_pcg_opts pcg;               /* for LES_SOLVER_PCG; tol is absolute unless rel_tol > 0 */
+    double rel_tol;                 /* > 0: PCG tol = rel_tol * ||b||_2 of this step */
+    int stat_max_iter;              /* Jacobi (reference 100) / GS-SOR sweeps (reference 200) */
+    double stat_tol;                /* max |dp| stop criterion (reference 1e-6) */
+    double omega;                   /* GS-SOR relaxation (reference 1.7) */
+    int want_tau;                   /* also store the (unused) SGS stress tensor */
+} les_step_params;
+
+typedef struct les_step_stats {
+    double dt;
+    int iters;            /* solver iterations / sweeps */
+    int outer;            /* MIXED defect-correction sweeps */
+    double residual;      /* PCG: final ||r||_2 */
+    double b_norm;        /* PCG: ||b||_2 */
+    int status;           /* les_status of the solve */
+} les_step_stats;
+
+/* ---- context ----------------------------------------------------------- */
+les_status les_create(const les_mesh* mesh, int device, les_ctx** out);
+void les_destroy(les_ctx* ctx);
+const char* les_last_error(const les_ctx* ctx);
+const char* les_status_string(int status);
+int les_abi_version(void);
+les_status les_sync(les_ctx* ctx);
+/* The context's cudaStream_t (as void*), for callers that order their own
+ * work or CUDA events against the library's. */
+void* les_stream(les_ctx* ctx);
+/* Device pointer of a slot (valid until the next les_momentum, which swaps
+ * U<->U_NEW etc., or les_destroy). */
+double* les_slot_ptr(les_ctx* ctx, int slot);
+uint8_t* les_mask_ptr(les_ctx* ctx);
+
+/* ---- host <-> device (the shim's Field sync points) --------------------- */
+les_status les_upload(les_ctx* ctx, int slot, const double* host);
+les_status les_download(les_ctx* ctx, int slot, double* host);
+/* is_solid (src/field.h:22) as one byte per cell, 0 or 1. */
+les_status les_upload_mask(les_ctx* ctx, const uint8_t* solid);
+les_status les_download_mask(les_ctx* ctx, uint8_t* solid);
+
+/* ---- step physics, src/main.cpp ---------------------------------------- */
+/* compute_adaptive_dt, src/main.cpp:208-250 (constants as arguments). */
+les_status les_adaptive_dt(les_ctx* ctx, double nu, double cfl_conv, double cfl_visc,
+                           double dt_max, double* dt);
+/* apply_velocity_BCs, src/main.cpp:323-410. */
+les_status les_velocity_bcs(les_ctx* ctx);
+/* compute_sgs_stress, src/main.cpp:423-472 (Cs is an argument; the
+ * reference hard-codes 0.18 at :425).  Writes nu_t on interior cells. */
+les_status les_sgs(les_ctx* ctx, double cs, int want_tau);
+/* apply_nut_BCs, src/main.cpp:483-547. */
+les_status les_nut_bcs(les_ctx* ctx);
+/* compute_sgs_stress + apply_nut_BCs fused into one pass. */
+les_status les_sgs_nut(les_ctx* ctx, double cs, int want_tau);
+/* tau_xx, xy, xz, yy, yz, zz (6*N doubles) of the last les_sgs(want_tau=1). */
+les_status les_download_tau(les_ctx* ctx, double* host6n);
+/* solve_momentum, src/main.cpp:563-659, including the u<->u_new swap. */
+les_status les_momentum(les_ctx* ctx, double dt, double nu);
+/* correct_velocity, src/main.cpp:671-714. */
+les_status les_correct_velocity(les_ctx* ctx, double dt, double rho);
+
+/* ---- pressure, src/pressure.cpp ---------------------------------------- */
+/* calculate_divergence(p_rhs, ...), src/pressure.cpp:256-329 (reads U_NEW..). */
+les_status les_divergence(les_ctx* ctx, double dt, double rho);
+/* build_b_vector(b, p_rhs, ...), src/pressure.cpp:566-599. */
+les_status les_build_b(les_ctx* ctx);
+/* apply_pressure_BCs, src/pressure.cpp:14-93. */
+les_status les_pressure_bcs(les_ctx* ctx);
+/* solve_pressure_jacobi, src/pressure.cpp:106-172 (reference: max_iter 100,
+ * tol 1e-6).  *sweeps gets the number of sweeps run. */
+les_status les_solve_jacobi(les_ctx* ctx, double dt, double rho, int max_iter, double tol,
+                            int* sweeps);
+/* solve_pressure_GS, src/pressure.cpp:186-247 (reference: omega 1.7, tol 1e-6),
+ * in hyperplane order, which reproduces the lexicographic update sequence. */
+les_status les_solve_gs(les_ctx* ctx, double dt, double rho, int max_iter, double omega,
+                        double tol, int* sweeps);
+/* build_stencil, src/pressure.cpp:608-699, from the mask uploaded now (the
+ * reference builds A before defining the obstacle, src/main.cpp:66-81; the
+ * caller reproduces that by calling this before les_upload_mask). */
+les_status les_build_stencil(les_ctx* ctx);
+/* Install an arbitrary 7-diagonal A (order c, n, s, e, w, t, b). */
+les_status les_set_stencil(les_ctx* ctx, const double* const* diag7);
+les_status les_get_stencil(les_ctx* ctx, double* const* diag7);
+/* build_ic_preconditioner, src/pressure.cpp:495-556, from the current A. */
+les_status les_build_ic(les_ctx* ctx);
+les_status les_set_ic_factor(les_ctx* ctx, const double* const* diag7);
+les_status les_get_ic_factor(les_ctx* ctx, double* const* diag7);
+/* estimate_lambda_max, src/pressure.cpp:917-955.  v0: start vector (N
+ * doubles) or NULL for std::mt19937(1337)/uniform(-1,1) drawn in index
+ * order (the reference's draw on one thread). */
+les_status les_lambda_max(les_ctx* ctx, int n_iter, const double* v0, double* lambda);
+/* solve_pressure_pcg (src/pressure.cpp:342-414) and
+ * solve_pressure_pcg_chebyshev (:762-835): solves A p = b in place in P. */
+les_status les_pcg(les_ctx* ctx, const les_pcg_opts* opts, les_pcg_result* res);
+
+/* ---- operators on slots ------------------------------------------------- */
+/* fast_apply_laplacian, src/pressure.cpp:709-746: out = A in. */
+les_status les_spmv(les_ctx* ctx, int in_slot, int out_slot);
+/* The preconditioner of opts applied once: out = M^-1 in
+ * (src/pressure.cpp:420-428, :442-482, :851-906). */
+les_status les_precond_apply(les_ctx* ctx, const les_pcg_opts* opts, int in_slot, int out_slot);
+/* parallel_dot, src/pressure.cpp:962-970. */
+les_status les_dot(les_ctx* ctx, int a_slot, int b_slot, double* out);
+
+/* ---- one full time step, src/main.cpp:115-144 --------------------------- */
+les_status les_step(les_ctx* ctx, const les_step_params* prm, les_step_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,331 @@
+// les_ctx.cu -- context lifetime, host<->device transfers, errors.
+//
+// Replaces the storage side of the reference Field (src/field.h:9-41): the
+// arrays live in HBM for the life of the context and the host copies only at
+// explicit sync points (the reference's checkpoint/VTK/statistics calls).
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "les_internal.cuh"
+
+using namespace les;
+
+namespace les {
+
+les_status fail(les_ctx* c, les_status st, const std::string& msg)
+{
+    if (c) c->err = msg;
+    return st;
+}
+
+les_status check_cuda(les_ctx* c, cudaError_t e, const char* what)
+{
+    if (e == cudaSuccess) return LES_OK;
+    return fail(c, LES_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+les_status check_launch(les_ctx* c, const char* what) { return check_cuda(c, cudaGetLastError(), what); }
+
+StencilView stencil_view(const les_ctx* c)
+{
+    StencilView v{};
+    if (c->stencil_mode == 1) {
+        v.code = c->code;
+        v.k = c->coef;
+    } else {
+        v.code = nullptr;
+        for (int q = 0; q < 7; ++q) v.d[q] = c->A[q];
+    }
+    return v;
+}
+
+int reduction_blocks(const Geo& g)
+{
+    dim3 gr = cell_grid(g);
+    return (int)(gr.x * gr.y * gr.z);
+}
+
+les_status ensure_work(les_ctx* c)
+{
+    if (c->w[0]) return LES_OK;
+    for (int q = 0; q < 8; ++q) {
+        cudaError_t e = cudaMalloc(&c->w[q], sizeof(double) * (size_t)c->g.n);
+        if (e != cudaSuccess) return check_cuda(c, e, "cudaMalloc(work)");
+        cudaMemsetAsync(c->w[q], 0, sizeof(double) * (size_t)c->g.n, c->stream);
+    }
+    return LES_OK;
+}
+
+les_status ensure_work32(les_ctx* c)
+{
+    if (c->f[0]) return LES_OK;
+    for (int q = 0; q < 8; ++q) {
+        cudaError_t e = cudaMalloc(&c->f[q], sizeof(float) * (size_t)c->g.n);
+        if (e != cudaSuccess) return check_cuda(c, e, "cudaMalloc(work32)");
+        cudaMemsetAsync(c->f[q], 0, sizeof(float) * (size_t)c->g.n, c->stream);
+    }
+    return LES_OK;
+}
+
+les_status read_state(les_ctx* c)
+{
+    les_status st = check_cuda(c, cudaMemcpyAsync(c->h_state, c->state, 2 * sizeof(SolverState),
+                                                  cudaMemcpyDeviceToHost, c->stream),
+                               "read state");
+    if (st) return st;
+    return check_cuda(c, cudaStreamSynchronize(c->stream), "sync");
+}
+
+}  // namespace les
+
+static bool mesh_ok(const les_mesh* m)
+{
+    if (!m || m->nx < 3 || m->ny < 3 || m->nz < 3) return false;
+    if (!(m->dx > 0 && m->dy > 0 && m->dz > 0)) return false;
+    long long n = (long long)m->nx * m->ny * m->nz;
+    return n < (1LL << 31) - 1024;
+}
+
+extern "C" {
+
+int les_abi_version(void) { return LES_ABI_VERSION; }
+
+const char* les_status_string(int s)
+{
+    switch (s) {
+    case LES_OK: return "ok";
+    case LES_NOT_CONVERGED: return "not converged";
+    case LES_NONFINITE: return "non-finite value";
+    case LES_BAD_ARG: return "bad argument";
+    case LES_CUDA_ERROR: return "CUDA error";
+    case LES_NO_DEVICE: return "no CUDA device";
+    case LES_TIMEOUT: return "device wait timed out";
+    default: return "unknown status";
+    }
+}
+
+const char* les_last_error(const les_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+les_status les_create(const les_mesh* mesh, int device, les_ctx** out)
+{
+    if (!out) return LES_BAD_ARG;
+    *out = nullptr;
+    if (!mesh_ok(mesh)) return LES_BAD_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return LES_NO_DEVICE;
+    }
+    if (device < 0 || device >= ndev) return LES_BAD_ARG;
+    les_ctx* c = new les_ctx();
+    c->device = device;
+    c->mesh = *mesh;
+    c->g.nx = mesh->nx; c->g.ny = mesh->ny; c->g.nz = mesh->nz;
+    c->g.n = mesh->nx * mesh->ny * mesh->nz;
+    c->g.si = mesh->ny * mesh->nz;
+    c->g.sj = mesh->nz;
+    les_status st = LES_OK;
+#define TRY(x, what)                                    \
+    do {                                                \
+        st = check_cuda(c, (x), what);                  \
+        if (st) { les_destroy(c); return st; }          \
+    } while (0)
+    TRY(cudaSetDevice(device), "cudaSetDevice");
+    TRY(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device), "attr");
+    TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    const size_t nb = sizeof(double) * (size_t)c->g.n;
+    for (int s = 0; s < LES_NSLOTS; ++s) {
+        TRY(cudaMalloc(&c->slot[s], nb), "cudaMalloc(field)");
+        TRY(cudaMemsetAsync(c->slot[s], 0, nb, c->stream), "memset");
+    }
+    TRY(cudaMalloc(&c->mask, (size_t)c->g.n), "cudaMalloc(mask)");
+    TRY(cudaMemsetAsync(c->mask, 0, (size_t)c->g.n, c->stream), "memset");
+    c->partials_len = (size_t)4 * (size_t)reduction_blocks(c->g) + 4096;
+    TRY(cudaMalloc(&c->partials, sizeof(double) * c->partials_len), "cudaMalloc(partials)");
+    TRY(cudaMalloc(&c->counters, sizeof(unsigned) * 32), "cudaMalloc(counters)");
+    TRY(cudaMemsetAsync(c->counters, 0, sizeof(unsigned) * 32, c->stream), "memset");
+    TRY(cudaMalloc(&c->state, 2 * sizeof(SolverState)), "cudaMalloc(state)");
+    TRY(cudaMemsetAsync(c->state, 0, 2 * sizeof(SolverState), c->stream), "memset");
+    TRY(cudaMallocHost(&c->h_state, 2 * sizeof(SolverState)), "cudaMallocHost");
+    TRY(cudaMalloc(&c->gsync, sizeof(unsigned) * 4), "cudaMalloc(gsync)");
+    TRY(cudaMemsetAsync(c->gsync, 0, sizeof(unsigned) * 4, c->stream), "memset");
+    TRY(cudaStreamSynchronize(c->stream), "sync");
+#undef TRY
+    *out = c;
+    return LES_OK;
+}
+
+void les_destroy(les_ctx* c)
+{
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto& p : c->slot) cudaFree(p);
+    for (auto& p : c->A) cudaFree(p);
+    for (auto& p : c->L) cudaFree(p);
+    for (auto& p : c->w) cudaFree(p);
+    for (auto& p : c->f) cudaFree(p);
+    for (auto& p : c->A32) cudaFree(p);
+    for (auto& p : c->L32) cudaFree(p);
+    cudaFree(c->mask);
+    cudaFree(c->solid_list);
+    cudaFree(c->code);
+    cudaFree(c->tau);
+    cudaFree(c->partials);
+    cudaFree(c->counters);
+    cudaFree(c->state);
+    cudaFree(c->gsync);
+    if (c->h_state) cudaFreeHost(c->h_state);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+les_status les_sync(les_ctx* c)
+{
+    if (!c) return LES_BAD_ARG;
+    return check_cuda(c, cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+}
+
+void* les_stream(les_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+double* les_slot_ptr(les_ctx* c, int s)
+{
+    if (!c || s < 0 || s >= LES_NSLOTS) return nullptr;
+    return c->slot[s];
+}
+
+uint8_t* les_mask_ptr(les_ctx* c) { return c ? c->mask : nullptr; }
+
+les_status les_upload(les_ctx* c, int s, const double* host)
+{
+    if (!c || s < 0 || s >= LES_NSLOTS || !host) return LES_BAD_ARG;
+    cudaSetDevice(c->device);
+    les_status st = check_cuda(c, cudaMemcpyAsync(c->slot[s], host, sizeof(double) * (size_t)c->g.n,
+                                                  cudaMemcpyHostToDevice, c->stream),
+                               "upload");
+    if (st) return st;
+    // the caller may reuse its buffer as soon as we return
+    return check_cuda(c, cudaStreamSynchronize(c->stream), "upload sync");
+}
+
+les_status les_download(les_ctx* c, int s, double* host)
+{
+    if (!c || s < 0 || s >= LES_NSLOTS || !host) return LES_BAD_ARG;
+    cudaSetDevice(c->device);
+    les_status st = check_cuda(c, cudaMemcpyAsync(host, c->slot[s], sizeof(double) * (size_t)c->g.n,
+                                                  cudaMemcpyDeviceToHost, c->stream),
+                               "download");
+    if (st) return st;
+    return check_cuda(c, cudaStreamSynchronize(c->stream), "download sync");
+}
+
+les_status les_upload_mask(les_ctx* c, const uint8_t* solid)
+{
+    if (!c || !solid) return LES_BAD_ARG;
+    cudaSetDevice(c->device);
+    const Geo& g = c->g;
+    std::vector<uint8_t> m01(g.n);
+    std::vector<int> list;
+    for (int id = 0; id < g.n; ++id) m01[id] = solid[id] ? 1 : 0;
+    for (int i = 1; i < g.nx - 1; ++i)
+        for (int j = 1; j < g.ny - 1; ++j)
+            for (int k = 1; k < g.nz - 1; ++k) {
+                int id = i * g.si + j * g.sj + k;
+                if (m01[id]) list.push_back(id);
+            }
+    les_status st = check_cuda(c, cudaMemcpyAsync(c->mask, m01.data(), (size_t)g.n, cudaMemcpyHostToDevice, c->stream),
+                               "upload mask");
+    if (st) return st;
+    cudaFree(c->solid_list);
+    c->solid_list = nullptr;
+    c->n_solid = (int)list.size();
+    if (c->n_solid) {
+        st = check_cuda(c, cudaMalloc(&c->solid_list, sizeof(int) * list.size()), "cudaMalloc(solid list)");
+        if (st) return st;
+        st = check_cuda(c, cudaMemcpyAsync(c->solid_list, list.data(), sizeof(int) * list.size(),
+                                           cudaMemcpyHostToDevice, c->stream),
+                        "upload solid list");
+        if (st) return st;
+    }
+    return check_cuda(c, cudaStreamSynchronize(c->stream), "upload mask sync");
+}
+
+les_status les_download_mask(les_ctx* c, uint8_t* solid)
+{
+    if (!c || !solid) return LES_BAD_ARG;
+    cudaSetDevice(c->device);
+    les_status st = check_cuda(c, cudaMemcpyAsync(solid, c->mask, (size_t)c->g.n, cudaMemcpyDeviceToHost, c->stream),
+                               "download mask");
+    if (st) return st;
+    return check_cuda(c, cudaStreamSynchronize(c->stream), "download mask sync");
+}
+
+les_status les_download_tau(les_ctx* c, double* host6n)
+{
+    if (!c || !host6n) return LES_BAD_ARG;
+    if (!c->tau) return fail(c, LES_BAD_ARG, "no stress tensor stored: call les_sgs with want_tau=1");
+    cudaSetDevice(c->device);
+    les_status st = check_cuda(c, cudaMemcpyAsync(host6n, c->tau, sizeof(double) * 6 * (size_t)c->g.n,
+                                                  cudaMemcpyDeviceToHost, c->stream),
+                               "download tau");
+    if (st) return st;
+    return check_cuda(c, cudaStreamSynchronize(c->stream), "sync");
+}
+
+static les_status put_diag7(les_ctx* c, double** dst, const double* const* src)
+{
+    const size_t nb = sizeof(double) * (size_t)c->g.n;
+    for (int q = 0; q < 7; ++q) {
+        if (!dst[q]) {
+            les_status st = check_cuda(c, cudaMalloc(&dst[q], nb), "cudaMalloc(diag)");
+            if (st) return st;
+        }
+        les_status st = check_cuda(c, cudaMemcpyAsync(dst[q], src[q], nb, cudaMemcpyHostToDevice, c->stream),
+                                   "upload diag");
+        if (st) return st;
+    }
+    return check_cuda(c, cudaStreamSynchronize(c->stream), "sync");
+}
+
+les_status les_set_stencil(les_ctx* c, const double* const* diag7)
+{
+    if (!c || !diag7) return LES_BAD_ARG;
+    for (int q = 0; q < 7; ++q)
+        if (!diag7[q]) return LES_BAD_ARG;
+    cudaSetDevice(c->device);
+    les_status st = put_diag7(c, c->A, diag7);
+    if (st) return st;
+    c->stencil_mode = 2;
+    c->A_valid = true;
+    return LES_OK;
+}
+
+les_status les_set_ic_factor(les_ctx* c, const double* const* diag7)
+{
+    if (!c || !diag7) return LES_BAD_ARG;
+    for (int q = 0; q < 7; ++q)
+        if (!diag7[q]) return LES_BAD_ARG;
+    cudaSetDevice(c->device);
+    les_status st = put_diag7(c, c->L, diag7);
+    if (st) return st;
+    c->have_L = true;
+    return LES_OK;
+}
+
+les_status les_get_ic_factor(les_ctx* c, double* const* diag7)
+{
+    if (!c || !diag7) return LES_BAD_ARG;
+    if (!c->have_L) return fail(c, LES_BAD_ARG, "no IC factor: call les_build_ic or les_set_ic_factor");
+    cudaSetDevice(c->device);
+    const size_t nb = sizeof(double) * (size_t)c->g.n;
+    for (int q = 0; q < 7; ++q) {
+        if (!diag7[q]) continue;
+        les_status st = check_cuda(c, cudaMemcpyAsync(diag7[q], c->L[q], nb, cudaMemcpyDeviceToHost, c->stream),
+                                   "download L");
+        if (st) return st;
+    }
+    return check_cuda(c, cudaStreamSynchronize(c->stream), "sync");
+}
+
+}  // extern "C"

@@ -1,0 +1,300 @@
+// les_internal.cuh -- shared device helpers and the context layout of the
+// GB300 les-model hot path.  Not part of the ABI.
+//
+// Layout in HBM: every field is one FP64 array of N = nx*ny*nz cells in the
+// reference order idx = i*ny*nz + j*nz + k (src/field.h:40), k contiguous.
+// The obstacle mask is one byte per cell.  The assembled matrix is kept as one
+// byte per cell (a stencil code, decoded to exact coefficients in registers)
+// when it was built on the device by les_build_stencil, or as seven FP64
+// diagonals when a caller installs an arbitrary matrix.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "les_gb300.h"
+
+namespace les {
+
+// ---- geometry -------------------------------------------------------------
+struct Geo {
+    int nx, ny, nz;
+    int n;        // nx*ny*nz (< 2^31)
+    int si, sj;   // strides of i and j
+};
+
+// Stencil block shape for per-cell kernels: 32 k x 8 j threads, grid.z = i.
+constexpr int TBK = 32;
+constexpr int TBJ = 8;
+
+inline dim3 cell_grid(const Geo& g) { return dim3((g.nz + TBK - 1) / TBK, (g.ny + TBJ - 1) / TBJ, g.nx); }
+inline dim3 cell_block() { return dim3(TBK, TBJ, 1); }
+
+// ---- stencil codes ---------------------------------------------------------
+// Code 0: identity row (solid cell or outlet, src/pressure.cpp:634-642).
+// Otherwise code-1 = xs + 5*(ys + 4*zs) where each state selects the
+// multiplier of the base coefficient for the two neighbours of one axis after
+// the ghost-doubling of src/pressure.cpp:663-696:
+//   x (w,e): 0:(1,1) 1:(0,2) 2:(1,0) 3:(0,0) 4:(2,0)
+//   y (s,n) and z (b,t): 0:(1,1) 1:(0,2) 2:(2,0) 3:(1,0)
+// Multipliers are packed two bits per state.
+constexpr unsigned XW_PACK = 1u | (0u << 2) | (1u << 4) | (0u << 6) | (2u << 8);
+constexpr unsigned XE_PACK = 1u | (2u << 2) | (0u << 4) | (0u << 6) | (0u << 8);
+constexpr unsigned YL_PACK = 1u | (0u << 2) | (2u << 4) | (1u << 6);  // s / b
+constexpr unsigned YH_PACK = 1u | (2u << 2) | (0u << 4) | (0u << 6);  // n / t
+
+// Exact coefficient values: c0 = 2/dx^2 + 2/dy^2 + 2/dz^2 summed in the
+// reference's order, m1 = -1/h^2, m2 = m1 + m1 per axis.
+struct StencilCoef {
+    double c0;
+    double x1, x2, y1, y2, z1, z2;
+};
+
+struct Coef7 {
+    double c, w, e, s, n, b, t;
+};
+
+__device__ __forceinline__ double sel(unsigned m, double v1, double v2)
+{
+    return m == 0u ? 0.0 : (m == 1u ? v1 : v2);
+}
+
+__device__ __forceinline__ Coef7 decode(unsigned code, const StencilCoef& k)
+{
+    Coef7 a;
+    if (code == 0u) {
+        a.c = 1.0; a.w = a.e = a.s = a.n = a.b = a.t = 0.0;
+        return a;
+    }
+    unsigned c = code - 1u;
+    unsigned xs = c % 5u, r = c / 5u;
+    unsigned ys = r & 3u, zs = r >> 2;
+    a.c = k.c0;
+    a.w = sel((XW_PACK >> (2 * xs)) & 3u, k.x1, k.x2);
+    a.e = sel((XE_PACK >> (2 * xs)) & 3u, k.x1, k.x2);
+    a.s = sel((YL_PACK >> (2 * ys)) & 3u, k.y1, k.y2);
+    a.n = sel((YH_PACK >> (2 * ys)) & 3u, k.y1, k.y2);
+    a.b = sel((YL_PACK >> (2 * zs)) & 3u, k.z1, k.z2);
+    a.t = sel((YH_PACK >> (2 * zs)) & 3u, k.z1, k.z2);
+    return a;
+}
+
+// Float twin for the FP32 inner solve (values rounded once from the FP64 ones).
+struct StencilCoefF {
+    float c0, x1, x2, y1, y2, z1, z2;
+};
+
+// Source of the seven diagonals: either codes (decoded) or stored arrays.
+struct StencilView {
+    const uint8_t* code;       // non-null: coded mode
+    StencilCoef k;
+    const double* d[7];        // stored mode: c, n, s, e, w, t, b
+    __device__ __forceinline__ Coef7 at(int id) const
+    {
+        if (code) return decode(code[id], k);
+        Coef7 a;
+        a.c = d[0][id]; a.n = d[1][id]; a.s = d[2][id]; a.e = d[3][id];
+        a.w = d[4][id]; a.t = d[5][id]; a.b = d[6][id];
+        return a;
+    }
+    __device__ __forceinline__ double diag(int id) const
+    {
+        if (code) return code[id] == 0 ? 1.0 : k.c0;
+        return d[0][id];
+    }
+};
+
+// ---- deterministic block reductions -----------------------------------------
+template <int NV>
+__device__ __forceinline__ void warp_sum(double (&v)[NV])
+{
+#pragma unroll
+    for (int q = 0; q < NV; ++q)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], o);
+}
+
+// Sums v over the block (fixed order); the result is valid in thread 0.
+// smem: NV*32 doubles.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double* smem)
+{
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int nthr = blockDim.x * blockDim.y * blockDim.z;
+    const int lane = tid & 31, warp = tid >> 5, nw = (nthr + 31) >> 5;
+    warp_sum<NV>(v);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) smem[q * 32 + warp] = v[q];
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) v[q] = lane < nw ? smem[q * 32 + lane] : 0.0;
+        warp_sum<NV>(v);
+    }
+}
+
+__device__ __forceinline__ double warp_max(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__device__ __forceinline__ int block_linear_id() { return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z); }
+__device__ __forceinline__ int block_count() { return gridDim.x * gridDim.y * gridDim.z; }
+
+// Two-stage deterministic sum: each block stores its partial; the block that
+// arrives last sums all partials in block order.  Returns true in every
+// thread of the last block, with the totals valid in its thread 0.
+template <int NV>
+__device__ bool last_block_sum(double (&v)[NV], double* partials, unsigned* counter, double* smem)
+{
+    __shared__ int am_last;
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int nthr = blockDim.x * blockDim.y * blockDim.z;
+    const int nb = block_count(), bid = block_linear_id();
+    block_sum<NV>(v, smem);
+    if (tid == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) partials[q * nb + bid] = v[q];
+        __threadfence();
+        unsigned t = atomicAdd(counter, 1u);
+        am_last = (t == (unsigned)nb - 1u);
+    }
+    __syncthreads();
+    if (!am_last) return false;
+    __threadfence();
+    double acc[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) acc[q] = 0.0;
+    for (int b = tid; b < nb; b += nthr)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) acc[q] += __ldcg(partials + q * nb + b);
+    block_sum<NV>(acc, smem);
+    if (tid == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) v[q] = acc[q];
+        *counter = 0u;
+    }
+    return true;
+}
+
+// ---- device-resident solver state -----------------------------------------
+struct SolverState {
+    double rho, alpha, beta, err, tol, pq, rr, rz, bnorm, maxdp;
+    double scal[8];   // misc scalars (dt, lambda, ...)
+    int k, done, iters, max_iter, status, buf, pad0, pad1;
+};
+
+// ---- bounded grid barrier for cooperative (co-resident) launches ------------
+struct GridSync {
+    unsigned* count;
+    unsigned* gen;
+    int* error;       // set to 1 when a wait gives up
+    unsigned nblocks;
+};
+
+__device__ __forceinline__ unsigned long long globaltimer_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Returns false (in every thread) once any block has given up waiting; the
+// caller then leaves the kernel.  A wait gives up after ~2 s.
+__device__ __forceinline__ bool grid_barrier(const GridSync& gs)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) {
+        volatile unsigned* vgen = gs.gen;
+        volatile int* verr = gs.error;
+        unsigned my_gen = *vgen;
+        __threadfence();
+        unsigned arrived = atomicAdd(gs.count, 1u);
+        int good = 1;
+        if (arrived == gs.nblocks - 1u) {
+            *gs.count = 0u;
+            __threadfence();
+            atomicAdd(gs.gen, 1u);
+        } else {
+            unsigned long long t0 = globaltimer_ns();
+            unsigned spins = 0;
+            while (*vgen == my_gen) {
+                if (*verr) { good = 0; break; }
+                if ((++spins & 255u) == 0u && globaltimer_ns() - t0 > 2000000000ull) {
+                    atomicExch(gs.error, 1);
+                    good = 0;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+        if (*verr) good = 0;
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+}  // namespace les
+
+// ---- the context -------------------------------------------------------------
+struct les_ctx {
+    int device = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    les_mesh mesh{};
+    les::Geo g{};
+    double* slot[LES_NSLOTS] = {};
+    uint8_t* mask = nullptr;
+    int* solid_list = nullptr;    // interior solid cells (for obstacle BC passes)
+    int n_solid = 0;
+    // matrix
+    int stencil_mode = 0;         // 0 none, 1 coded, 2 stored
+    uint8_t* code = nullptr;
+    double* A[7] = {};
+    bool A_valid = false;         // A[] holds the current matrix (stored, or expanded codes)
+    les::StencilCoef coef{};
+    double* L[7] = {};
+    bool have_L = false;
+    double* tau = nullptr;
+    // work vectors (FP64)
+    double* w[8] = {};
+    // FP32 work vectors for the mixed-precision inner solve, and FP32 copies
+    // of a stored A / of the IC factor for it
+    float* f[8] = {};
+    float* A32[7] = {};
+    float* L32[7] = {};
+    // reductions / state
+    double* partials = nullptr;
+    size_t partials_len = 0;
+    unsigned* counters = nullptr;  // 32 last-block counters (one per reduction site)
+    les::SolverState* state = nullptr;
+    les::SolverState* h_state = nullptr;  // pinned mirror
+    unsigned* gsync = nullptr;            // count, gen, error
+    std::string err;
+};
+
+namespace les {
+
+les_status fail(les_ctx* c, les_status st, const std::string& msg);
+les_status check_cuda(les_ctx* c, cudaError_t e, const char* what);
+les_status check_launch(les_ctx* c, const char* what);
+StencilView stencil_view(const les_ctx* c);
+les_status ensure_work(les_ctx* c);
+les_status ensure_work32(les_ctx* c);
+les_status read_state(les_ctx* c);
+int reduction_blocks(const Geo& g);
+
+// kernels shared across translation units (les_pressure.cu)
+les_status spmv_dev(les_ctx* c, const double* in, double* out);
+les_status dot_dev(les_ctx* c, const double* a, const double* b, double* out_host);
+
+}  // namespace les

@@ -1,0 +1,326 @@
+"""ctypes binding of the les_gb300 C ABI (include/les_gb300.h).
+
+This is how the tests and bench.py drive the CUDA library: every call goes
+through the same extern "C" entry points a C/C++ host (or the reference-API
+shim) would use.  There is no fallback: if libles_gb300.so is missing or no
+GPU is present the calls raise.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(HERE)
+LIB_PATH = os.path.join(PKG, "libles_gb300.so")
+
+# status codes
+OK, NOT_CONVERGED, NONFINITE, BAD_ARG, CUDA_ERROR, NO_DEVICE, TIMEOUT = range(7)
+# slots
+U, V, W, U_NEW, V_NEW, W_NEW, P, P_RHS, NU_T, B = range(10)
+SLOTS = {"u": U, "v": V, "w": W, "u_new": U_NEW, "v_new": V_NEW, "w_new": W_NEW, "p": P,
+         "p_rhs": P_RHS, "nu_t": NU_T, "b": B}
+# solvers, preconditioners, precision
+SOLVER_PCG, SOLVER_JACOBI, SOLVER_GS = 0, 1, 2
+PC_JACOBI, PC_IC, PC_CHEBYSHEV, PC_IC_A = 0, 1, 2, 3
+FP64, MIXED = 0, 1
+DIAGS = ("c", "n", "s", "e", "w", "t", "b")
+
+_dp = C.POINTER(C.c_double)
+_u8 = C.POINTER(C.c_uint8)
+
+
+class LesError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("les_gb300 status %d: %s" % (status, msg))
+        self.status = status
+
+
+class Mesh(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double)]
+
+    @property
+    def n(self):
+        return self.nx * self.ny * self.nz
+
+
+class PcgOpts(C.Structure):
+    _fields_ = [("precond", C.c_int), ("max_iter", C.c_int), ("tol", C.c_double),
+                ("lambda_min", C.c_double), ("lambda_max", C.c_double), ("degree", C.c_int),
+                ("precision", C.c_int), ("inner_rtol", C.c_double), ("inner_max_iter", C.c_int),
+                ("max_outer", C.c_int)]
+
+
+class PcgResult(C.Structure):
+    _fields_ = [("iters", C.c_int), ("outer", C.c_int), ("residual", C.c_double)]
+
+
+class StepParams(C.Structure):
+    _fields_ = [("nu", C.c_double), ("rho", C.c_double), ("cs", C.c_double),
+                ("cfl_conv", C.c_double), ("cfl_visc", C.c_double), ("dt_max", C.c_double),
+                ("dt_fixed", C.c_double), ("solver", C.c_int), ("pcg", PcgOpts),
+                ("rel_tol", C.c_double), ("stat_max_iter", C.c_int), ("stat_tol", C.c_double),
+                ("omega", C.c_double), ("want_tau", C.c_int)]
+
+
+class StepStats(C.Structure):
+    _fields_ = [("dt", C.c_double), ("iters", C.c_int), ("outer", C.c_int),
+                ("residual", C.c_double), ("b_norm", C.c_double), ("status", C.c_int)]
+
+
+def pcg_opts(precond=PC_JACOBI, max_iter=1000, tol=1e-6, lambda_min=0.0, lambda_max=0.0, degree=5,
+             precision=FP64, inner_rtol=1e-4, inner_max_iter=0, max_outer=50):
+    return PcgOpts(precond, max_iter, tol, lambda_min, lambda_max, degree, precision, inner_rtol,
+                   inner_max_iter, max_outer)
+
+
+def step_params(**kw):
+    """Reference defaults (src/main.cpp:83-87, :137, :210-212, :425;
+    src/pressure.cpp:134, :195)."""
+    d = dict(nu=1e-5, rho=1.2, cs=0.18, cfl_conv=0.4, cfl_visc=0.2, dt_max=1e-4, dt_fixed=0.0,
+             solver=SOLVER_PCG, rel_tol=0.0, stat_max_iter=100, stat_tol=1e-6, omega=1.7, want_tau=0)
+    pcg = kw.pop("pcg", None) or pcg_opts(precond=PC_IC_A, max_iter=1000, tol=1e-6)
+    d.update(kw)
+    return StepParams(d["nu"], d["rho"], d["cs"], d["cfl_conv"], d["cfl_visc"], d["dt_max"],
+                      d["dt_fixed"], d["solver"], pcg, d["rel_tol"], d["stat_max_iter"], d["stat_tol"],
+                      d["omega"], d["want_tau"])
+
+
+_lib = None
+
+
+def load(path=None):
+    """Loads libles_gb300.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise FileNotFoundError("%s is missing: run les-model_gb300/build_ext.py (or "
+                                "__graft_entry__.build())" % p)
+    L = C.CDLL(p)
+    L.les_last_error.restype = C.c_char_p
+    L.les_status_string.restype = C.c_char_p
+    L.les_stream.restype = C.c_void_p
+    L.les_slot_ptr.restype = C.c_void_p
+    L.les_mask_ptr.restype = C.c_void_p
+    L.les_create.argtypes = [C.POINTER(Mesh), C.c_int, C.POINTER(C.c_void_p)]
+    L.les_destroy.argtypes = [C.c_void_p]
+    for name in ("les_last_error", "les_sync", "les_stream", "les_velocity_bcs", "les_nut_bcs",
+                 "les_build_b", "les_pressure_bcs", "les_build_stencil", "les_build_ic"):
+        getattr(L, name).argtypes = [C.c_void_p]
+    if path is None:
+        _lib = L
+    return L
+
+
+def exported_symbols():
+    """Names the header declares (parsed from include/les_gb300.h)."""
+    import re
+    hdr = os.path.join(os.path.dirname(PKG), "include", "les_gb300.h")
+    src = open(hdr).read()
+    return sorted(set(re.findall(r"^\s*(?:[A-Za-z_][\w\s\*]*?)\b(les_\w+)\s*\(", src, re.M)))
+
+
+def _arr(a, dtype=np.float64):
+    a = np.ascontiguousarray(a, dtype=dtype)
+    return a
+
+
+class Context:
+    """One device context (a Field mirror + pressure system on one GPU)."""
+
+    def __init__(self, mesh, device=0, lib=None):
+        self.lib = lib or load()
+        self.mesh = mesh
+        self.n = mesh.n
+        h = C.c_void_p()
+        st = self.lib.les_create(C.byref(mesh), device, C.byref(h))
+        if st != OK:
+            raise LesError(st, self.lib.les_status_string(st).decode())
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.les_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _chk(self, st, allow=(OK,)):
+        if st not in allow:
+            raise LesError(st, self.lib.les_last_error(self.h).decode())
+        return st
+
+    # --- plumbing
+    @property
+    def stream(self):
+        return self.lib.les_stream(self.h)
+
+    def slot_ptr(self, slot):
+        return self.lib.les_slot_ptr(self.h, SLOTS.get(slot, slot))
+
+    def sync(self):
+        self._chk(self.lib.les_sync(self.h))
+
+    def upload(self, slot, a):
+        a = _arr(a)
+        assert a.size == self.n
+        self._chk(self.lib.les_upload(self.h, SLOTS.get(slot, slot), a.ctypes.data_as(_dp)))
+
+    def upload_ptr(self, slot, ptr):
+        self._chk(self.lib.les_upload(self.h, SLOTS.get(slot, slot), C.cast(ptr, _dp)))
+
+    def download(self, slot, out=None):
+        out = np.empty(self.n) if out is None else out
+        self._chk(self.lib.les_download(self.h, SLOTS.get(slot, slot), out.ctypes.data_as(_dp)))
+        return out
+
+    def download_ptr(self, slot, ptr):
+        self._chk(self.lib.les_download(self.h, SLOTS.get(slot, slot), C.cast(ptr, _dp)))
+
+    def upload_mask(self, m):
+        m = _arr(m, np.uint8)
+        assert m.size == self.n
+        self._chk(self.lib.les_upload_mask(self.h, m.ctypes.data_as(_u8)))
+
+    def download_mask(self):
+        out = np.empty(self.n, np.uint8)
+        self._chk(self.lib.les_download_mask(self.h, out.ctypes.data_as(_u8)))
+        return out
+
+    def upload_fields(self, f):
+        for k, v in f.items():
+            if k == "solid":
+                self.upload_mask(v)
+            elif k in SLOTS:
+                self.upload(k, v)
+
+    def download_fields(self, keys=("u", "v", "w", "u_new", "v_new", "w_new", "p", "p_rhs", "nu_t")):
+        return {k: self.download(k) for k in keys}
+
+    # --- step physics
+    def adaptive_dt(self, nu, cfl_conv=0.4, cfl_visc=0.2, dt_max=1e-4):
+        dt = C.c_double()
+        self._chk(self.lib.les_adaptive_dt(self.h, C.c_double(nu), C.c_double(cfl_conv),
+                                           C.c_double(cfl_visc), C.c_double(dt_max), C.byref(dt)))
+        return dt.value
+
+    def velocity_bcs(self):
+        self._chk(self.lib.les_velocity_bcs(self.h))
+
+    def sgs(self, cs, want_tau=False):
+        self._chk(self.lib.les_sgs(self.h, C.c_double(cs), int(want_tau)))
+
+    def nut_bcs(self):
+        self._chk(self.lib.les_nut_bcs(self.h))
+
+    def sgs_nut(self, cs, want_tau=False):
+        self._chk(self.lib.les_sgs_nut(self.h, C.c_double(cs), int(want_tau)))
+
+    def download_tau(self):
+        out = np.empty(6 * self.n)
+        self._chk(self.lib.les_download_tau(self.h, out.ctypes.data_as(_dp)))
+        return out
+
+    def momentum(self, dt, nu):
+        self._chk(self.lib.les_momentum(self.h, C.c_double(dt), C.c_double(nu)))
+
+    def correct_velocity(self, dt, rho):
+        self._chk(self.lib.les_correct_velocity(self.h, C.c_double(dt), C.c_double(rho)))
+
+    # --- pressure
+    def divergence(self, dt, rho):
+        self._chk(self.lib.les_divergence(self.h, C.c_double(dt), C.c_double(rho)))
+
+    def build_b(self):
+        self._chk(self.lib.les_build_b(self.h))
+
+    def pressure_bcs(self):
+        self._chk(self.lib.les_pressure_bcs(self.h))
+
+    def solve_jacobi(self, dt, rho, max_iter=100, tol=1e-6):
+        it = C.c_int()
+        self._chk(self.lib.les_solve_jacobi(self.h, C.c_double(dt), C.c_double(rho), int(max_iter),
+                                            C.c_double(tol), C.byref(it)))
+        return it.value
+
+    def solve_gs(self, dt, rho, max_iter=200, omega=1.7, tol=1e-6):
+        it = C.c_int()
+        self._chk(self.lib.les_solve_gs(self.h, C.c_double(dt), C.c_double(rho), int(max_iter),
+                                        C.c_double(omega), C.c_double(tol), C.byref(it)))
+        return it.value
+
+    def build_stencil(self):
+        self._chk(self.lib.les_build_stencil(self.h))
+
+    def _d7(self, d):
+        arrs = [_arr(d[k]) for k in DIAGS]
+        ptrs = (_dp * 7)(*[a.ctypes.data_as(_dp) for a in arrs])
+        return ptrs, arrs
+
+    def set_stencil(self, d):
+        ptrs, keep = self._d7(d)
+        self._chk(self.lib.les_set_stencil(self.h, ptrs))
+
+    def get_stencil(self):
+        d = {k: np.empty(self.n) for k in DIAGS}
+        ptrs, _ = self._d7(d)
+        self._chk(self.lib.les_get_stencil(self.h, ptrs))
+        return d
+
+    def build_ic(self):
+        self._chk(self.lib.les_build_ic(self.h))
+
+    def set_ic_factor(self, d):
+        ptrs, keep = self._d7(d)
+        self._chk(self.lib.les_set_ic_factor(self.h, ptrs))
+
+    def get_ic_factor(self):
+        d = {k: np.empty(self.n) for k in DIAGS}
+        ptrs, _ = self._d7(d)
+        self._chk(self.lib.les_get_ic_factor(self.h, ptrs))
+        return d
+
+    def lambda_max(self, n_iter=20, v0=None):
+        lam = C.c_double()
+        if v0 is not None:
+            v0 = _arr(v0)
+        self._chk(self.lib.les_lambda_max(self.h, int(n_iter),
+                                          v0.ctypes.data_as(_dp) if v0 is not None else None,
+                                          C.byref(lam)))
+        return lam.value
+
+    def pcg(self, opts):
+        r = PcgResult()
+        st = self.lib.les_pcg(self.h, C.byref(opts), C.byref(r))
+        self._chk(st, allow=(OK, NOT_CONVERGED, NONFINITE))
+        return st, r
+
+    def spmv(self, src, dst):
+        self._chk(self.lib.les_spmv(self.h, SLOTS.get(src, src), SLOTS.get(dst, dst)))
+
+    def precond_apply(self, opts, src, dst):
+        self._chk(self.lib.les_precond_apply(self.h, C.byref(opts), SLOTS.get(src, src),
+                                             SLOTS.get(dst, dst)))
+
+    def dot(self, a, b):
+        out = C.c_double()
+        self._chk(self.lib.les_dot(self.h, SLOTS.get(a, a), SLOTS.get(b, b), C.byref(out)))
+        return out.value
+
+    def step(self, params):
+        s = StepStats()
+        self._chk(self.lib.les_step(self.h, C.byref(params), C.byref(s)))
+        return s

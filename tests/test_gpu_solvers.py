@@ -1,0 +1,142 @@
+"""Solver-level parity: PCG (Jacobi, Chebyshev, IC(L), IC with A as shipped)
+in FP64 against the golden fixtures and the oracle, and the mixed-precision
+solve against the FP64 solve.
+
+The GPU reduces dot products in a different order from the reference's
+sequential sum, so a PCG iterate differs from the reference by rounding that
+CG then propagates.  Bars (written per test): x within 1e-10 relative after a
+short run; iteration counts within +-1 where the reference converges."""
+import numpy as np
+import pytest
+
+from conftest import GRIDS, golden_mesh, load_golden, maxrel
+
+import les_cases
+import les_gb300 as G
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+X_RTOL_SHORT = 1e-10    # x after a few iterations
+X_RTOL_CONVERGED = 1e-8 # x of a converged solve (tol 1e-8*||b||)
+
+
+@pytest.fixture(scope="module", params=GRIDS)
+def g(request):
+    return load_golden(request.param)
+
+
+def _A(d, tag):
+    return {k: d["out_%s_%s" % (tag, k)].copy() for k in O.DIAGS}
+
+
+VARIANTS = [("shipped", G.PC_IC_A, O.PC_IC, 60), ("cheb", G.PC_CHEBYSHEV, O.PC_CHEB, 300),
+            ("jac", G.PC_JACOBI, O.PC_JACOBI, 300), ("icL", G.PC_IC, O.PC_IC, 300)]
+
+
+def _gpu_pcg(m, A0, L0, b, x0, pc, tol, max_iter, lmin, lmax, precision=G.FP64, **kw):
+    with G.Context(G.Mesh(m.nx, m.ny, m.nz, m.dx, m.dy, m.dz)) as c:
+        c.upload_mask(np.zeros(m.n, np.uint8))
+        c.build_stencil()
+        if L0 is not None:
+            c.set_ic_factor(L0)
+        c.upload("b", b)
+        c.upload("p", x0)
+        st, r = c.pcg(G.pcg_opts(precond=pc, max_iter=max_iter, tol=tol, lambda_min=lmin,
+                                 lambda_max=lmax, degree=4, precision=precision, **kw))
+        return st, r, c.download("p")
+
+
+@pytest.mark.parametrize("variant", VARIANTS, ids=[v[0] for v in VARIANTS])
+def test_pcg_short_runs_match_oracle(oracle_lib, g, variant):
+    tag, gpc, opc, _ = variant
+    m = golden_mesh(g)
+    A0 = _A(g, "A0")
+    L0 = _A(g, "L0")
+    lmax, lmin = (float(x) for x in g["out_lmax"])
+    b = g["out_b"]
+    tol = float(g["pcg_tol"][0])
+    for iters in (1, 5, 12):
+        x_ref = g["in_p"].copy()
+        it_ref, _ = oracle_lib.pcg(m, A0, b, x_ref, opc, L=(A0 if tag == "shipped" else L0), lmin=lmin,
+                                   lmax=lmax, degree=4, max_iter=iters, tol=tol)
+        st, r, x = _gpu_pcg(m, A0, L0 if tag == "icL" else None, b, g["in_p"], gpc, tol, iters, lmin, lmax)
+        assert r.iters == it_ref
+        assert maxrel(x, x_ref) < X_RTOL_SHORT, (tag, iters, maxrel(x, x_ref))
+
+
+@pytest.mark.parametrize("variant", VARIANTS, ids=[v[0] for v in VARIANTS])
+def test_pcg_full_runs_against_golden(g, variant):
+    tag, gpc, _, max_iter = variant
+    m = golden_mesh(g)
+    A0 = _A(g, "A0")
+    L0 = _A(g, "L0")
+    lmax, lmin = (float(x) for x in g["out_lmax"])
+    idx = [v[0] for v in VARIANTS].index(tag)
+    it_ref = int(g["out_pcg_iters"][idx])
+    st, r, x = _gpu_pcg(m, A0, L0 if tag == "icL" else None, g["out_b"], g["in_p"], gpc,
+                        float(g["pcg_tol"][0]), max_iter, lmin, lmax)
+    x_ref = g["out_pcg_%s_x" % tag]
+    if it_ref < max_iter:   # the reference converged
+        assert st == G.OK
+        assert abs(r.iters - it_ref) <= 1, (r.iters, it_ref)
+        assert maxrel(x, x_ref) < X_RTOL_CONVERGED, maxrel(x, x_ref)
+    else:                   # it hit the cap: so must we, ending near the same iterate
+        assert r.iters == max_iter and st == G.NOT_CONVERGED
+        assert np.all(np.isfinite(x)) == np.all(np.isfinite(x_ref))
+
+
+def _small_system(seed=5):
+    """The small configuration's pressure system after one momentum step."""
+    shape, h, solid, f = les_cases.case("small", seed)
+    m = G.Mesh(*shape, h, h, h)
+    with G.Context(m) as c:
+        c.upload_mask(np.zeros(m.n, np.uint8))
+        c.build_stencil()
+        c.upload_fields(f)
+        c.upload_mask(solid)
+        c.sgs_nut(les_cases.CS)
+        c.momentum(1e-4, les_cases.NU)
+        c.velocity_bcs()
+        c.divergence(1e-4, les_cases.RHO)
+        c.build_b()
+        b = c.download("b")
+    return m, solid, b
+
+
+def test_pcg_jacobi_converges_like_oracle_on_small_config(oracle_lib):
+    m, solid, b = _small_system()
+    om = O.Mesh(m.nx, m.ny, m.nz, m.dx, m.dy, m.dz)
+    A0 = oracle_lib.build_stencil(om, np.zeros(m.n, np.uint8))
+    tol = 1e-8 * np.linalg.norm(b)
+    x_ref = np.zeros(m.n)
+    it_ref, _ = oracle_lib.pcg(om, A0, b, x_ref, O.PC_JACOBI, max_iter=1000, tol=tol)
+    st, r, x = _gpu_pcg(om, A0, None, b, np.zeros(m.n), G.PC_JACOBI, tol, 1000, 0, 0)
+    assert it_ref < 1000 and st == G.OK
+    assert abs(r.iters - it_ref) <= 1, (r.iters, it_ref)
+    assert maxrel(x, x_ref) < X_RTOL_CONVERGED, maxrel(x, x_ref)
+
+
+@pytest.mark.parametrize("pc", [G.PC_CHEBYSHEV, G.PC_JACOBI, G.PC_IC])
+def test_mixed_precision_matches_fp64(pc):
+    """FP32 inner / FP64 defect correction reaches the same relative residual
+    1e-8 as the FP64 solve; pressure agrees with the FP64 solution to 1e-6."""
+    m, solid, b = _small_system()
+    om = O.Mesh(m.nx, m.ny, m.nz, m.dx, m.dy, m.dz)
+    tol = 1e-8 * np.linalg.norm(b)
+    lmin, lmax = 3 * np.pi ** 2, 0.0
+    with G.Context(m) as c:
+        c.upload_mask(np.zeros(m.n, np.uint8))
+        c.build_stencil()
+        lmax = c.lambda_max(20)
+    L0 = None
+    if pc == G.PC_IC:
+        import oracle
+        Lo = oracle.Oracle().ic_build(om, oracle.Oracle().build_stencil(om, np.zeros(m.n, np.uint8)))
+        L0 = Lo
+    st64, r64, x64 = _gpu_pcg(om, None, L0, b, np.zeros(m.n), pc, tol, 5000, lmin, lmax)
+    st32, r32, x32 = _gpu_pcg(om, None, L0, b, np.zeros(m.n), pc, tol, 20000, lmin, lmax,
+                              precision=G.MIXED, inner_rtol=1e-4)
+    assert st64 == G.OK and st32 == G.OK, (st64, st32, r64.iters, r32.iters, r32.outer)
+    assert r32.residual < tol
+    assert maxrel(x32, x64) < 1e-6, maxrel(x32, x64)
