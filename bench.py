@@ -1,0 +1,409 @@
+#!/usr/bin/env python
+"""bench.py -- throughput of the les-model time step on GB300.
+
+Workload (default): the 256x128x128 configuration (obstacle scaled 4x,
+u = 1 + U(-0.01, 0.01) noise), one step = SGS nu_t + momentum + velocity BCs +
+divergence RHS + pressure solve to relative residual 1e-8 + projection +
+velocity BCs.  The pressure solve is Chebyshev(4)-PCG, mixed precision (FP32
+inner PCG, FP64 defect correction); the plain FP64 GPU path runs the same
+trajectory beside it for the FP64-vs-mixed comparison and per-step errors.
+
+Metric: Mcell-steps/s = cells x steps / device seconds (CUDA events on the
+library's stream, L2 flushed before every timed step).  Also reported:
+  e2e           the same metric through the C ABI from pinned host buffers,
+                host<->device copies of the step's state inside the timing;
+  roofline      HBM bytes/s of the dominant kernel against the measured copy
+                bandwidth (MEASURED_PEAKS.json);
+  cpu_baseline  the CPU oracle (OpenMP, all host threads) on a bounded sample
+                of the same step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Multi-GPU (torchrun): independent replicas, one per GPU (the step has no
+exchange to shard); rank 0 prints the max-over-ranks result.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for sub in (os.path.join(ROOT, "les-model_gb300", "py"), os.path.join(ROOT, "les-model_gb300"),
+            os.path.join(ROOT, "oracle")):
+    if sub not in sys.path:
+        sys.path.insert(0, sub)
+
+import numpy as np  # noqa: E402
+
+METRIC = "Mcell-steps/s @256x128x128, mixed vs FP64 GPU at div<=1e-8; HBM GB/s % peak"
+UNIT = "Mcell-steps/s"
+FALLBACK_HBM_GBS = 6800.0
+
+# FP64 Chebyshev(4)-PCG iterations per step for the default workload, as
+# measured by the FP64 GPU path (whose counts match the reference's within
+# +-1 in the parity tests); used by the reference arm to extrapolate its
+# bounded per-step sample to a full solve.
+REF_ITERS = {"large": 300, "small": 150, "xlarge": 500}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
+    ap.add_argument("--workload", default="large", choices=("small", "large", "xlarge"))
+    ap.add_argument("--precond", default="cheb", choices=("cheb", "jacobi", "ic"))
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--cpu-iters", type=int, default=12, help="PCG iterations in the CPU sample")
+    ap.add_argument("--seed", type=int, default=1234)
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[q] for r in rows for q in range(4) if r[5 + q].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# algorithmic HBM bytes per cell of one launch of each profiled kernel
+def alg_bytes_per_cell(name, degree):
+    if name == "inner_cheb_f32":
+        # zin, r, code, pout, zout (+ pin after the first step of each apply)
+        steps = max(degree - 1, 1)
+        return (17.0 + 21.0 * (steps - 1)) / steps
+    return {"inner_spmv_f32": 17.0, "inner_update_f32": 28.0, "spmv_f64": 17.0, "update_f64": 48.0,
+            "cheb_f64": 41.0, "outer_resid_f64": 21.0}.get(name)
+
+
+def pc_code(G, name):
+    return {"cheb": G.PC_CHEBYSHEV, "jacobi": G.PC_JACOBI, "ic": G.PC_IC}[name]
+
+
+def make_ctx(G, les_cases, shape, h, solid, f, dev, precond):
+    m = G.Mesh(*shape, h, h, h)
+    c = G.Context(m, dev)
+    c.upload_mask(np.zeros(m.n, np.uint8))
+    c.build_stencil()            # src/main.cpp:66: A before the obstacle
+    if precond == "ic":
+        c.build_ic()
+    lmax = c.lambda_max(20)      # :74
+    c.upload_mask(solid)         # :81
+    c.upload_fields(f)
+    return c, lmax
+
+
+def step_params(G, les_cases, precond, lmax, precision):
+    pc = pc_code(G, precond)
+    if precision == G.MIXED:
+        opts = G.pcg_opts(precond=pc, max_iter=50000, lambda_min=3 * np.pi ** 2, lambda_max=lmax, degree=4,
+                          precision=G.MIXED, inner_rtol=1e-4, inner_max_iter=5000, max_outer=40)
+    else:
+        opts = G.pcg_opts(precond=pc, max_iter=10000, lambda_min=3 * np.pi ** 2, lambda_max=lmax, degree=4)
+    return G.step_params(nu=les_cases.NU, rho=les_cases.RHO, cs=les_cases.CS, cfl_conv=les_cases.CFL_CONV,
+                         cfl_visc=les_cases.CFL_VISC, dt_max=les_cases.DT_MAX, solver=G.SOLVER_PCG,
+                         rel_tol=1e-8, pcg=opts)
+
+
+def cpu_sample(shape, h, solid, f, precond, iters_per_step, sample_iters):
+    """Times the oracle (OpenMP, all host threads) on one step's physics and
+    `sample_iters` PCG iterations of the same system; returns the per-step
+    time extrapolated to `iters_per_step` solver iterations."""
+    import les_cases
+    import oracle as O
+    orc = O.Oracle()
+    threads = os.cpu_count() or 1
+    orc.set_threads(threads)
+    m = O.Mesh(*shape, h, h, h)
+    n = m.n
+    A0 = orc.build_stencil(m, np.zeros(n, np.uint8))
+    L0 = orc.ic_build(m, A0) if precond == "ic" else None
+    u, v, w = f["u"].copy(), f["v"].copy(), f["w"].copy()
+    nt = np.zeros(n)
+    un, vn, wn = np.zeros(n), np.zeros(n), np.zeros(n)
+    dt = les_cases.DT_MAX
+    t0 = time.perf_counter()
+    orc.sgs(m, les_cases.CS, u, v, w, nt)
+    orc.nut_bcs(m, nt, solid)
+    orc.momentum(m, dt, les_cases.NU, u, v, w, nt, un, vn, wn)
+    orc.velocity_bcs(m, un, vn, wn, solid)
+    div = np.zeros(n)
+    b = np.zeros(n)
+    orc.divergence(m, dt, les_cases.RHO, u, v, w, solid, div)
+    orc.build_b(m, div, solid, b)
+    orc.correct_velocity(m, dt, les_cases.RHO, np.zeros(n), un, vn, wn)
+    orc.velocity_bcs(m, un, vn, wn, solid)
+    t_phys = time.perf_counter() - t0
+    pc = {"cheb": O.PC_CHEB, "jacobi": O.PC_JACOBI, "ic": O.PC_IC}[precond]
+    lmin, lmax = 3 * np.pi ** 2, 2.0e5
+
+    def run(k):
+        best = None
+        for _ in range(2):
+            x = np.zeros(n)
+            t = time.perf_counter()
+            orc.pcg(m, A0, b, x, pc, L=L0, lmin=lmin, lmax=lmax, degree=4, max_iter=k, tol=0.0)
+            t = time.perf_counter() - t
+            best = t if best is None else min(best, t)
+        return best
+
+    t_a = run(1)
+    t_b = run(1 + sample_iters)
+    t_iter = max(t_b - t_a, 1e-9) / sample_iters
+    step_s = t_phys + t_a + iters_per_step * t_iter
+    return {"step_s": step_s, "t_phys_s": t_phys, "t_iter_s": t_iter, "threads": threads,
+            "sampled_s": t_phys + t_a + t_b}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    import les_cases
+    shape, h, solid, f = les_cases.case(args.workload, args.seed)
+    n = int(np.prod(shape))
+    iters = REF_ITERS[args.workload]
+    vals = []
+    s = None
+    for q in range(args.warmup + args.steps):
+        s = cpu_sample(shape, h, solid, f, args.precond, iters, max(2, args.cpu_iters // 2))
+        if q >= args.warmup:
+            vals.append(n / s["step_s"] / 1e6)
+    value = statistics.mean(vals)
+    sample = ("each step: the oracle's SGS+momentum+BCs+divergence+projection and %d %s-PCG FP64 iterations "
+              "timed at %s, extrapolated to %d iterations per step" %
+              (max(2, args.cpu_iters // 2), args.precond, "x".join(map(str, shape)), iters))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n / (value * 1e6),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": "x".join(map(str, shape)) + " " + args.precond + "-PCG FP64",
+                                             "solver": args.precond},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": s["threads"], "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import les_cases
+    import les_gb300 as G
+
+    rank, world, local = dist_env()
+    dev = local if world > 1 else 0
+    torch.cuda.set_device(dev)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        pg = dist
+    shape, h, solid, f = les_cases.case(args.workload, args.seed)
+    n = int(np.prod(shape))
+    ctx, lmax = make_ctx(G, les_cases, shape, h, solid, f, dev, args.precond)
+    prm = step_params(G, les_cases, args.precond, lmax, G.MIXED)
+    ctx64 = None
+    if not args.no_fp64:
+        ctx64, _ = make_ctx(G, les_cases, shape, h, solid, f, dev, args.precond)
+        prm64 = step_params(G, les_cases, args.precond, lmax, G.FP64)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")   # 256 MiB > L2
+
+    def l2_flush():
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        ctx.step(prm)
+        if ctx64:
+            ctx64.step(prm64)
+    ctx.sync()
+    if ctx64:
+        ctx64.sync()
+
+    rec = dict(ms=[], ms64=[], iters=[], outer=[], iters64=[], rres=[], rres64=[], err=[])
+    clocks = Clocks(dev)
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ctx.profile(1)
+    launches0 = ctx.launch_count()
+    wall0 = time.perf_counter()
+    for s in range(args.steps):
+        l2_flush()
+        ctx.mark(0)
+        st = ctx.step(prm)
+        ctx.mark(1)
+        rec["ms"].append(ctx.elapsed(0, 1))
+        rec["iters"].append(st.iters)
+        rec["outer"].append(st.outer)
+        rec["rres"].append(st.residual / st.b_norm if st.b_norm > 0 else 0.0)
+        if ctx64:
+            l2_flush()
+            ctx64.mark(0)
+            s64 = ctx64.step(prm64)
+            ctx64.mark(1)
+            rec["ms64"].append(ctx64.elapsed(0, 1))
+            rec["iters64"].append(s64.iters)
+            rec["rres64"].append(s64.residual / s64.b_norm if s64.b_norm > 0 else 0.0)
+            e = {}
+            for k in ("u", "v", "w", "p"):
+                a, b = ctx.download(k), ctx64.download(k)
+                e[k] = float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+            rec["err"].append(e)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    launches = ctx.launch_count() - launches0
+    prof = ctx.profile_all()
+    ctx.profile(0)
+    clk = clocks.stop()
+    t_dev = sum(rec["ms"]) / 1e3
+    if pg:
+        t = torch.tensor([t_dev], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        t_dev = float(t.item())
+    value = world * n * args.steps / t_dev / 1e6
+
+    # ---- end to end through the C ABI with pinned host buffers
+    in_keys = ("u", "v", "w", "u_new", "v_new", "w_new", "p", "nu_t")
+    out_keys = ("u", "v", "w", "u_new", "v_new", "w_new", "p", "p_rhs", "nu_t")
+    host = {k: torch.empty(n, dtype=torch.float64).pin_memory() for k in set(in_keys) | set(out_keys)}
+    for k in host:
+        ctx.download_ptr(k, host[k].data_ptr())
+    e2e_t = 0.0
+    for s in range(args.steps):
+        t0 = time.perf_counter()
+        for k in in_keys:
+            ctx.upload_ptr(k, host[k].data_ptr())
+        ctx.step(prm)
+        for k in out_keys:
+            ctx.download_ptr(k, host[k].data_ptr())
+        e2e_t += time.perf_counter() - t0
+    e2e = {"value": world * n * args.steps / e2e_t / 1e6, "unit": UNIT,
+           "h2d_bytes_per_step": 8 * n * len(in_keys), "d2h_bytes_per_step": 8 * n * len(out_keys)}
+
+    # ---- roofline of the dominant kernel (CUDA events during the timed steps)
+    peak, peak_kind = measured_peak()
+    roof = None
+    if prof:
+        name, (cnt, ms) = max(prof.items(), key=lambda kv: kv[1][1])
+        bpc = alg_bytes_per_cell(name, 4)
+        traffic = None
+        tp = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(tp):
+            try:
+                traffic = json.load(open(tp)).get(name, {}).get("dram_bytes_per_cell")
+                traffic = traffic * n if traffic else None
+            except Exception:
+                traffic = None
+        if bpc:
+            achieved = bpc * n * cnt / (ms / 1e3) / 1e9
+            roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                    "alg_bytes_per_launch": bpc * n, "launches": cnt, "avg_launch_us": 1e3 * ms / cnt,
+                    "share_of_step": ms / (sum(rec["ms"]) or 1.0),
+                    "kernels": {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()}}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 outer",
+            "data": "synthetic",
+            "config": {"workload": "%s %s obstacle, %s(4)-PCG mixed FP32/FP64 to rel residual 1e-8" %
+                                   (args.workload, "x".join(map(str, shape)), args.precond),
+                       "cells": n, "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "flushed (256 MiB write) before every timed step"},
+            "e2e": e2e, "gpu_launches": launches, "wall_s": wall,
+            "iters_inner_mean": statistics.mean(rec["iters"]), "outer_mean": statistics.mean(rec["outer"]),
+            "rel_residual_max": max(rec["rres"]), "roofline": roof, "clocks": clk}
+    if ctx64:
+        t64 = sum(rec["ms64"]) / 1e3
+        line["fp64"] = {"value": n * args.steps / t64 / 1e6, "ms_per_step": 1e3 * t64 / args.steps,
+                        "iters_mean": statistics.mean(rec["iters64"]), "rel_residual_max": max(rec["rres64"])}
+        line["speedup_vs_fp64"] = value / line["fp64"]["value"]
+        line["err_vs_fp64_max"] = {k: max(e[k] for e in rec["err"]) for k in ("u", "v", "w", "p")}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        iters = statistics.mean(rec["iters64"]) if rec["iters64"] else REF_ITERS[args.workload]
+        s = cpu_sample(shape, h, solid, f, args.precond, iters, args.cpu_iters)
+        line["cpu_baseline"] = {"value": n / s["step_s"] / 1e6, "unit": UNIT, "cores": s["threads"],
+                                "kind": "port",
+                                "sample": "oracle physics pass + %d FP64 %s-PCG iterations at %s (%.1f s), "
+                                          "extrapolated to %.0f iterations/step (the FP64 path's count)" %
+                                          (args.cpu_iters, args.precond, "x".join(map(str, shape)),
+                                           s["sampled_s"], iters)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if ctx64:
+        ctx64.close()
+    if pg:
+        pg.barrier()
+        pg.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -201,6 +201,21 @@ les_status les_precond_apply(les_ctx* ctx, const les_pcg_opts* opts, int in_slot
 /* parallel_dot, src/pressure.cpp:962-970. */
 les_status les_dot(les_ctx* ctx, int a_slot, int b_slot, double* out);
 
+/* ---- accounting (no reference counterpart) ------------------------------ */
+/* Number of kernels this context has launched so far. */
+unsigned long long les_launch_count(const les_ctx* ctx);
+/* CUDA-event timing of the solver's hot kernels: enable=1 starts a fresh
+ * record, 0 stops recording. */
+les_status les_profile(les_ctx* ctx, int enable);
+/* Launch count and summed device time (ms) of one profiled kernel id
+ * (0..7, names from les_profile_name). */
+les_status les_profile_read(les_ctx* ctx, int kernel_id, int* launches, double* total_ms);
+const char* les_profile_name(int kernel_id);
+/* Records CUDA event slot `mark` (0..63) on the context's stream. */
+les_status les_mark(les_ctx* ctx, int mark);
+/* Device time between two recorded marks, in ms (waits for mark1). */
+les_status les_elapsed(les_ctx* ctx, int mark0, int mark1, double* ms);
+
 /* ---- one full time step, src/main.cpp:115-144 --------------------------- */
 les_status les_step(les_ctx* ctx, const les_step_params* prm, les_step_stats* stats);
 

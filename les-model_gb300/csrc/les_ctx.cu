@@ -68,6 +68,20 @@ les_status ensure_work32(les_ctx* c)
     return LES_OK;
 }
 
+// Records the start event of a profiled launch; *e1 gets its end event.
+void prof_begin(les_ctx* c, int id, cudaEvent_t* e1)
+{
+    const size_t r = c->prof_id.size();
+    while (c->prof_ev.size() < 2 * r + 2) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) { *e1 = nullptr; return; }
+        c->prof_ev.push_back(e);
+    }
+    c->prof_id.push_back(id);
+    cudaEventRecord(c->prof_ev[2 * r], c->stream);
+    *e1 = c->prof_ev[2 * r + 1];
+}
+
 les_status read_state(les_ctx* c)
 {
     les_status st = check_cuda(c, cudaMemcpyAsync(c->h_state, c->state, 2 * sizeof(SolverState),
@@ -177,6 +191,8 @@ void les_destroy(les_ctx* c)
     cudaFree(c->state);
     cudaFree(c->gsync);
     if (c->h_state) cudaFreeHost(c->h_state);
+    for (auto& e : c->prof_ev) cudaEventDestroy(e);
+    for (auto& e : c->marks) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -311,6 +327,73 @@ les_status les_set_ic_factor(les_ctx* c, const double* const* diag7)
     if (st) return st;
     c->have_L = true;
     return LES_OK;
+}
+
+unsigned long long les_launch_count(const les_ctx* c) { return c ? c->launches : 0ull; }
+
+les_status les_mark(les_ctx* c, int mark)
+{
+    if (!c || mark < 0 || mark >= 64) return LES_BAD_ARG;
+    cudaSetDevice(c->device);
+    if (c->marks.empty()) {
+        c->marks.resize(64);
+        for (auto& e : c->marks) {
+            les_status st = check_cuda(c, cudaEventCreate(&e), "cudaEventCreate");
+            if (st) return st;
+        }
+    }
+    return check_cuda(c, cudaEventRecord(c->marks[mark], c->stream), "cudaEventRecord");
+}
+
+les_status les_elapsed(les_ctx* c, int mark0, int mark1, double* ms)
+{
+    if (!c || !ms || mark0 < 0 || mark1 < 0 || mark0 >= 64 || mark1 >= 64 || c->marks.empty()) return LES_BAD_ARG;
+    cudaSetDevice(c->device);
+    les_status st = check_cuda(c, cudaEventSynchronize(c->marks[mark1]), "cudaEventSynchronize");
+    if (st) return st;
+    float t = 0.f;
+    st = check_cuda(c, cudaEventElapsedTime(&t, c->marks[mark0], c->marks[mark1]), "cudaEventElapsedTime");
+    *ms = t;
+    return st;
+}
+
+les_status les_profile(les_ctx* c, int enable)
+{
+    if (!c) return LES_BAD_ARG;
+    cudaSetDevice(c->device);
+    les_status st = check_cuda(c, cudaStreamSynchronize(c->stream), "sync");
+    if (st) return st;
+    if (enable) c->prof_id.clear();
+    c->prof_on = enable ? 1 : 0;
+    return LES_OK;
+}
+
+les_status les_profile_read(les_ctx* c, int kernel_id, int* launches, double* total_ms)
+{
+    if (!c || kernel_id < 0 || kernel_id >= PROF_N) return LES_BAD_ARG;
+    cudaSetDevice(c->device);
+    les_status st = check_cuda(c, cudaStreamSynchronize(c->stream), "sync");
+    if (st) return st;
+    int cnt = 0;
+    double ms = 0.0;
+    for (size_t r = 0; r < c->prof_id.size(); ++r) {
+        if (c->prof_id[r] != kernel_id) continue;
+        float t = 0.f;
+        st = check_cuda(c, cudaEventElapsedTime(&t, c->prof_ev[2 * r], c->prof_ev[2 * r + 1]), "event time");
+        if (st) return st;
+        ms += t;
+        ++cnt;
+    }
+    if (launches) *launches = cnt;
+    if (total_ms) *total_ms = ms;
+    return LES_OK;
+}
+
+const char* les_profile_name(int kernel_id)
+{
+    static const char* names[PROF_N] = {"inner_cheb_f32", "inner_spmv_f32", "inner_update_f32", "spmv_f64",
+                                        "update_f64",     "cheb_f64",       "outer_resid_f64",  "ic_apply"};
+    return (kernel_id >= 0 && kernel_id < PROF_N) ? names[kernel_id] : "unknown";
 }
 
 les_status les_get_ic_factor(les_ctx* c, double* const* diag7)

@@ -13,6 +13,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "les_gb300.h"
 
@@ -280,7 +281,51 @@ struct les_ctx {
     les::SolverState* h_state = nullptr;  // pinned mirror
     unsigned* gsync = nullptr;            // count, gen, error
     std::string err;
+    // accounting: kernel launches issued by this context, and optional CUDA
+    // event timing of the solver's hot kernels (les_profile)
+    unsigned long long launches = 0;
+    int prof_on = 0;
+    std::vector<cudaEvent_t> prof_ev;     // pool, two per recorded launch
+    std::vector<int> prof_id;             // kernel id of each recorded pair
+    std::vector<cudaEvent_t> marks;       // les_mark slots
 };
+
+namespace les {
+
+// Profiled kernel ids (les_profile_read).
+enum ProfId {
+    PROF_IN_CHEB = 0,   // FP32 inner Chebyshev step (mixed path)
+    PROF_IN_SPMV = 1,   // FP32 inner SpMV + p update + p.q
+    PROF_IN_UPDATE = 2, // FP32 inner e/r update + ||r|| (+ first preconditioner stage)
+    PROF_SPMV64 = 3,    // FP64 SpMV + p.q
+    PROF_UPDATE64 = 4,  // FP64 x/r update + ||r||
+    PROF_CHEB64 = 5,    // FP64 Chebyshev step
+    PROF_OUTER = 6,     // FP64 outer residual of the mixed path
+    PROF_IC = 7,        // IC(0) wavefront apply
+    PROF_N = 8
+};
+
+void prof_begin(les_ctx* c, int id, cudaEvent_t* e1);
+
+template <typename... KArgs, typename... Args>
+inline void launch(les_ctx* c, void (*k)(KArgs...), dim3 grid, dim3 block, Args... args)
+{
+    k<<<grid, block, 0, c->stream>>>(args...);
+    ++c->launches;
+}
+
+// Same, with CUDA events around the launch while profiling is on.
+template <typename... KArgs, typename... Args>
+inline void launch_p(les_ctx* c, int pid, void (*k)(KArgs...), dim3 grid, dim3 block, Args... args)
+{
+    cudaEvent_t e1 = nullptr;
+    if (c->prof_on) prof_begin(c, pid, &e1);
+    k<<<grid, block, 0, c->stream>>>(args...);
+    ++c->launches;
+    if (e1) cudaEventRecord(e1, c->stream);
+}
+
+}  // namespace les
 
 namespace les {
 

@@ -344,7 +344,7 @@ les_status ensure_f32_copy(les_ctx* c, float** dst, double* const* src)
             les_status st = check_cuda(c, cudaMalloc(&dst[q], sizeof(float) * (size_t)n), "cudaMalloc(f32 copy)");
             if (st) return st;
         }
-        k_to_f<<<(n + 255) / 256, 256, 0, c->stream>>>(n, src[q], dst[q]);
+        launch(c, k_to_f, (n + 255) / 256, 256, n, src[q], dst[q]);
     }
     return check_launch(c, "f32 copy");
 }
@@ -372,19 +372,19 @@ static les_status inner_precond(les_ctx* c, const les_pcg_opts* o, ViewF A, floa
         for (int kq = 1; kq <= steps; ++kq) {
             double beta = (cc * alpha / 2.0) * (cc * alpha / 2.0);
             alpha = 1.0 / (d - beta);
-            k_in_cheb<<<gr, bl, 0, c->stream>>>(g, A, (float)alpha, (float)beta, r, zb[cur], kq == 1 ? nullptr : pbuf,
+            launch_p(c, PROF_IN_CHEB, k_in_cheb, gr, bl, g, A, (float)alpha, (float)beta, r, zb[cur], kq == 1 ? nullptr : pbuf,
                                                 pbuf, zb[cur ^ 1], kq == steps, c->partials, c->counters + 12, in,
                                                 skip_done);
             cur ^= 1;
         }
         if (steps == 0)
-            k_in_dot_beta<<<gr, bl, 0, c->stream>>>(g, r, z, c->partials, c->counters + 13, in, init);
+            launch(c, k_in_dot_beta, gr, bl, g, r, z, c->partials, c->counters + 13, in, init);
         return check_launch(c, "inner chebyshev");
     }
     // IC: wavefront solve in FP32, then r.z
     les_status st = ic_apply_dev32(c, r, z, L32, skip_done ? in : nullptr);
     if (st) return st;
-    k_in_dot_beta<<<gr, bl, 0, c->stream>>>(g, r, z, c->partials, c->counters + 13, in, init);
+    launch(c, k_in_dot_beta, gr, bl, g, r, z, c->partials, c->counters + 13, in, init);
     return check_launch(c, "inner ic");
 }
 
@@ -428,8 +428,8 @@ les_status pcg_mixed_impl(les_ctx* c, const les_pcg_opts* o, les_pcg_result* res
     const int inner_cap = o->inner_max_iter > 0 ? o->inner_max_iter : o->max_iter;
     const int max_outer = o->max_outer > 0 ? o->max_outer : 50;
 
-    k_set_outer<<<1, 1, 0, c->stream>>>(out, o->tol, keep_tol);
-    k_outer_resid<<<gr, bl, 0, c->stream>>>(g, A, x, b, r, c->partials, c->counters + 8, out, 0);
+    launch(c, k_set_outer, 1, 1, out, o->tol, keep_tol);
+    launch_p(c, PROF_OUTER, k_outer_resid, gr, bl, g, A, x, b, r, c->partials, c->counters + 8, out, 0);
     st = check_launch(c, "outer residual");
     if (st) return st;
     st = read_state(c);
@@ -437,33 +437,33 @@ les_status pcg_mixed_impl(les_ctx* c, const les_pcg_opts* o, les_pcg_result* res
     int outer = 0;
     while (!c->h_state[0].done && outer < max_outer && c->h_state[0].iters < o->max_iter) {
         // ---- inner FP32 PCG on A e = r, e0 = 0
-        k_inner_init<<<1, 1, 0, c->stream>>>(in, out, o->inner_rtol, inner_cap);
+        launch(c, k_inner_init, 1, 1, in, out, o->inner_rtol, inner_cap);
         if (mode == 2) {
-            k_zero_f<<<gr, bl, 0, c->stream>>>(g, e);
+            launch(c, k_zero_f, gr, bl, g, e);
             st = inner_precond(c, o, A32, r, z, in, L32, 0, 1);
         } else {
             // Chebyshev: the first z must land where the recurrence expects it
             int steps = o->degree - 1;
             float* z0 = (mode == 1 && steps % 2 == 1) ? c->f[6] : z;
-            k_in_pc0<<<gr, bl, 0, c->stream>>>(g, A32, mode, alpha0, r, z0, e, c->partials, c->counters + 9, in);
+            launch(c, k_in_pc0, gr, bl, g, A32, mode, alpha0, r, z0, e, c->partials, c->counters + 9, in);
             if (mode == 1 && steps > 0) st = inner_precond(c, o, A32, r, z, in, L32, 0, 1);
         }
         if (st) return st;
         int cur = 0, launched = 0, batch = 4;
         for (;;) {
             for (int it = 0; it < batch; ++it) {
-                k_in_spmv<<<gr, bl, 0, c->stream>>>(g, A32, z, pb[cur], pb[cur ^ 1], q, launched + it == 0 ? 1 : 0,
+                launch_p(c, PROF_IN_SPMV, k_in_spmv, gr, bl, g, A32, z, pb[cur], pb[cur ^ 1], q, launched + it == 0 ? 1 : 0,
                                                     c->partials, c->counters + 10, in);
                 cur ^= 1;
                 if (mode == 1) {
                     int steps = o->degree - 1;
                     float* z0 = (steps % 2 == 1) ? c->f[6] : z;
-                    k_in_update<<<gr, bl, 0, c->stream>>>(g, A32, mode, alpha0, e, r, pb[cur], q, z0, c->partials,
+                    launch_p(c, PROF_IN_UPDATE, k_in_update, gr, bl, g, A32, mode, alpha0, e, r, pb[cur], q, z0, c->partials,
                                                           c->counters + 11, in, out, o->max_iter);
                     if (steps > 0) st = inner_precond(c, o, A32, r, z, in, L32, 1, 0);
-                    else k_in_dot_beta<<<gr, bl, 0, c->stream>>>(g, r, z, c->partials, c->counters + 13, in, 0);
+                    else launch(c, k_in_dot_beta, gr, bl, g, r, z, c->partials, c->counters + 13, in, 0);
                 } else {
-                    k_in_update<<<gr, bl, 0, c->stream>>>(g, A32, mode, alpha0, e, r, pb[cur], q, z, c->partials,
+                    launch_p(c, PROF_IN_UPDATE, k_in_update, gr, bl, g, A32, mode, alpha0, e, r, pb[cur], q, z, c->partials,
                                                           c->counters + 11, in, out, o->max_iter);
                     if (mode == 2) st = inner_precond(c, o, A32, r, z, in, L32, 1, 0);
                 }
@@ -478,9 +478,9 @@ les_status pcg_mixed_impl(les_ctx* c, const les_pcg_opts* o, les_pcg_result* res
             batch = batch < 32 ? batch * 2 : 32;
         }
         // ---- correction and the new FP64 residual
-        k_x_add<<<gr, bl, 0, c->stream>>>(g, x, e);
+        launch(c, k_x_add, gr, bl, g, x, e);
         ++outer;
-        k_outer_resid<<<gr, bl, 0, c->stream>>>(g, A, x, b, r, c->partials, c->counters + 8, out, outer);
+        launch_p(c, PROF_OUTER, k_outer_resid, gr, bl, g, A, x, b, r, c->partials, c->counters + 8, out, outer);
         st = check_launch(c, "outer correction");
         if (st) return st;
         st = read_state(c);

@@ -280,10 +280,10 @@ namespace les {
 les_status velocity_bcs_dev(les_ctx* c)
 {
     const Geo& g = c->g;
-    k_velocity_faces<<<cell_grid(g), cell_block(), 0, c->stream>>>(g, c->mask, c->slot[LES_U],
+    launch(c, k_velocity_faces, cell_grid(g), cell_block(), g, c->mask, c->slot[LES_U],
                                                                     c->slot[LES_V], c->slot[LES_W]);
     if (c->n_solid)
-        k_zero_list3<<<(c->n_solid + 255) / 256, 256, 0, c->stream>>>(
+        launch(c, k_zero_list3, (c->n_solid + 255) / 256, 256, 
             c->solid_list, c->n_solid, c->slot[LES_U], c->slot[LES_V], c->slot[LES_W]);
     return check_launch(c, "velocity bcs");
 }
@@ -300,7 +300,7 @@ les_status sgs_nut_dev(les_ctx* c, double cs, int want_tau)
     // src/main.cpp:426 and :461 compute it
     double delta = std::pow(c->mesh.dx * c->mesh.dy * c->mesh.dz, 1.0 / 3.0);
     double cs2 = std::pow(cs * delta, 2);
-    k_sgs_nut<<<cell_grid(g), cell_block(), 0, c->stream>>>(
+    launch(c, k_sgs_nut, cell_grid(g), cell_block(), 
         g, step_const(c->mesh), cs2, c->slot[LES_U], c->slot[LES_V], c->slot[LES_W], c->mask,
         c->slot[LES_NU_T], want_tau ? c->tau : nullptr);
     return check_launch(c, "sgs+nut");
@@ -309,7 +309,7 @@ les_status sgs_nut_dev(les_ctx* c, double cs, int want_tau)
 les_status momentum_dev(les_ctx* c, double dt, double nu)
 {
     const Geo& g = c->g;
-    k_momentum<<<cell_grid(g), cell_block(), 0, c->stream>>>(
+    launch(c, k_momentum, cell_grid(g), cell_block(), 
         g, step_const(c->mesh), dt, nu, c->slot[LES_U], c->slot[LES_V], c->slot[LES_W],
         c->slot[LES_NU_T], c->slot[LES_U_NEW], c->slot[LES_V_NEW], c->slot[LES_W_NEW]);
     std::swap(c->slot[LES_U], c->slot[LES_U_NEW]);
@@ -321,7 +321,7 @@ les_status momentum_dev(les_ctx* c, double dt, double nu)
 les_status correct_dev(les_ctx* c, double dt, double rho)
 {
     const Geo& g = c->g;
-    k_correct<<<cell_grid(g), cell_block(), 0, c->stream>>>(g, step_const(c->mesh), dt / rho,
+    launch(c, k_correct, cell_grid(g), cell_block(), g, step_const(c->mesh), dt / rho,
                                                              c->slot[LES_P], c->slot[LES_U],
                                                              c->slot[LES_V], c->slot[LES_W]);
     return check_launch(c, "correct velocity");
@@ -333,7 +333,7 @@ les_status adaptive_dt_dev(les_ctx* c, double nu, double cfl_conv, double cfl_vi
     double min_dx = c->mesh.dx;
     if (c->mesh.dy < min_dx) min_dx = c->mesh.dy;
     if (c->mesh.dz < min_dx) min_dx = c->mesh.dz;
-    k_dt<<<cell_grid(g), cell_block(), 0, c->stream>>>(
+    launch(c, k_dt, cell_grid(g), cell_block(), 
         g, c->slot[LES_U], c->slot[LES_V], c->slot[LES_W], c->slot[LES_NU_T], c->partials,
         c->counters + 0, c->state, nu, cfl_conv, cfl_visc, dt_max, min_dx);
     return check_launch(c, "adaptive dt");
@@ -375,7 +375,7 @@ les_status les_sgs(les_ctx* c, double cs, int want_tau)
     }
     double delta = std::pow(c->mesh.dx * c->mesh.dy * c->mesh.dz, 1.0 / 3.0);
     double cs2 = std::pow(cs * delta, 2);
-    k_sgs<<<cell_grid(g), cell_block(), 0, c->stream>>>(g, step_const(c->mesh), cs2, c->slot[LES_U],
+    launch(c, k_sgs, cell_grid(g), cell_block(), g, step_const(c->mesh), cs2, c->slot[LES_U],
                                                          c->slot[LES_V], c->slot[LES_W],
                                                          c->slot[LES_NU_T], want_tau ? c->tau : nullptr);
     return check_launch(c, "sgs");
@@ -386,9 +386,9 @@ les_status les_nut_bcs(les_ctx* c)
     if (!c) return LES_BAD_ARG;
     cudaSetDevice(c->device);
     const Geo& g = c->g;
-    k_nut_faces<<<cell_grid(g), cell_block(), 0, c->stream>>>(g, c->slot[LES_NU_T]);
+    launch(c, k_nut_faces, cell_grid(g), cell_block(), g, c->slot[LES_NU_T]);
     if (c->n_solid)
-        k_zero_list3<<<(c->n_solid + 255) / 256, 256, 0, c->stream>>>(c->solid_list, c->n_solid,
+        launch(c, k_zero_list3, (c->n_solid + 255) / 256, 256, c->solid_list, c->n_solid,
                                                                         c->slot[LES_NU_T], nullptr, nullptr);
     return check_launch(c, "nut bcs");
 }

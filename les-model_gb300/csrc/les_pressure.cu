@@ -483,14 +483,14 @@ namespace les {
 les_status spmv_dev(les_ctx* c, const double* in, double* out)
 {
     if (!c->stencil_mode) return fail(c, LES_BAD_ARG, "no matrix: call les_build_stencil or les_set_stencil");
-    k_spmv<<<cell_grid(c->g), cell_block(), 0, c->stream>>>(c->g, stencil_view(c), in, out, c->partials,
+    launch(c, k_spmv, cell_grid(c->g), cell_block(), c->g, stencil_view(c), in, out, c->partials,
                                                              c->counters + 1, c->state, DOT_NONE);
     return check_launch(c, "spmv");
 }
 
 les_status dot_dev(les_ctx* c, const double* a, const double* b, double* out_host)
 {
-    k_dot<<<cell_grid(c->g), cell_block(), 0, c->stream>>>(c->g, a, b, c->partials, c->counters + 2,
+    launch(c, k_dot, cell_grid(c->g), cell_block(), c->g, a, b, c->partials, c->counters + 2,
                                                             c->state, RD_SCAL0, 0);
     les_status st = check_launch(c, "dot");
     if (st) return st;
@@ -503,7 +503,7 @@ les_status dot_dev(les_ctx* c, const double* a, const double* b, double* out_hos
 les_status div_b_dev(les_ctx* c, double dt, double rho, double rel_tol)
 {
     const les_mesh& m = c->mesh;
-    k_div_b<<<cell_grid(c->g), cell_block(), 0, c->stream>>>(
+    launch(c, k_div_b, cell_grid(c->g), cell_block(), 
         c->g, rho / dt, 1.0 / (2.0 * m.dx), 1.0 / (2.0 * m.dy), 1.0 / (2.0 * m.dz), 1.0 / m.dx,
         1.0 / m.dy, 1.0 / m.dz, c->slot[LES_U_NEW], c->slot[LES_V_NEW], c->slot[LES_W_NEW], c->mask,
         c->slot[LES_P_RHS], c->slot[LES_B], c->partials, c->counters + 3, c->state, rel_tol);
@@ -512,9 +512,9 @@ les_status div_b_dev(les_ctx* c, double dt, double rho, double rel_tol)
 
 les_status pressure_bcs_dev(les_ctx* c, double* p)
 {
-    k_pbc_faces<<<cell_grid(c->g), cell_block(), 0, c->stream>>>(c->g, p, p);
+    launch(c, k_pbc_faces, cell_grid(c->g), cell_block(), c->g, p, p);
     if (c->n_solid)
-        k_pbc_obstacle<<<(c->n_solid + 255) / 256, 256, 0, c->stream>>>(c->g, c->solid_list, c->n_solid,
+        launch(c, k_pbc_obstacle, (c->n_solid + 255) / 256, 256, c->g, c->solid_list, c->n_solid,
                                                                           c->mask, p);
     return check_launch(c, "pressure bcs");
 }
@@ -527,7 +527,7 @@ les_status precond_dev(les_ctx* c, const les_pcg_opts* o, const double* r, doubl
     StencilView A = stencil_view(c);
     switch (o->precond) {
     case LES_PC_JACOBI:
-        k_jacobi_pc<<<cell_grid(g), cell_block(), 0, c->stream>>>(g, A, r, z, c->state, skip_done);
+        launch(c, k_jacobi_pc, cell_grid(g), cell_block(), g, A, r, z, c->state, skip_done);
         return check_launch(c, "jacobi pc");
     case LES_PC_CHEBYSHEV: {
         if (o->degree < 1) return fail(c, LES_BAD_ARG, "Chebyshev degree must be >= 1");
@@ -540,12 +540,12 @@ les_status precond_dev(les_ctx* c, const les_pcg_opts* o, const double* r, doubl
         // ping-pong z so that the last write lands in `z`
         double* zb[2] = {z, c->w[6]};
         int cur = (steps % 2 == 0) ? 0 : 1;
-        k_cheb0<<<cell_grid(g), cell_block(), 0, c->stream>>>(g, alpha, r, zb[cur], c->state, skip_done);
+        launch(c, k_cheb0, cell_grid(g), cell_block(), g, alpha, r, zb[cur], c->state, skip_done);
         double* pbuf = c->w[7];
         for (int kq = 1; kq <= steps; ++kq) {
             double beta = (cc * alpha / 2.0) * (cc * alpha / 2.0);
             alpha = 1.0 / (d - beta);
-            k_cheb_step<<<cell_grid(g), cell_block(), 0, c->stream>>>(
+            launch_p(c, PROF_CHEB64, k_cheb_step, cell_grid(g), cell_block(), 
                 g, A, alpha, beta, r, zb[cur], kq == 1 ? nullptr : pbuf, pbuf, zb[cur ^ 1], c->state,
                 skip_done);
             cur ^= 1;
@@ -577,7 +577,7 @@ les_status ensure_stored_A(les_ctx* c)
             les_status st = check_cuda(c, cudaMalloc(&c->A[q], nb), "cudaMalloc(A)");
             if (st) return st;
         }
-    k_expand_stencil<<<cell_grid(c->g), cell_block(), 0, c->stream>>>(
+    launch(c, k_expand_stencil, cell_grid(c->g), cell_block(), 
         c->g, stencil_view(c), c->A[0], c->A[1], c->A[2], c->A[3], c->A[4], c->A[5], c->A[6]);
     // keep using the codes for the SpMV; the arrays are an exact copy
     c->A_valid = true;
@@ -601,12 +601,12 @@ les_status pcg_fp64(les_ctx* c, const les_pcg_opts* o, les_pcg_result* res, int 
     double *x = c->slot[LES_P], *b = c->slot[LES_B];
     double *r = c->w[0], *z = c->w[1], *p = c->w[2], *q = c->w[3];
     const dim3 gr = cell_grid(g), bl = cell_block();
-    k_init_state<<<1, 1, 0, c->stream>>>(c->state, o->tol, o->max_iter, keep_tol);
-    k_spmv<<<gr, bl, 0, c->stream>>>(g, A, x, q, c->partials, c->counters + 1, c->state, DOT_NONE);
-    k_resid<<<gr, bl, 0, c->stream>>>(g, b, q, r, c->partials, c->counters + 4, c->state);
+    launch(c, k_init_state, 1, 1, c->state, o->tol, o->max_iter, keep_tol);
+    launch(c, k_spmv, gr, bl, g, A, x, q, c->partials, c->counters + 1, c->state, DOT_NONE);
+    launch(c, k_resid, gr, bl, g, b, q, r, c->partials, c->counters + 4, c->state);
     st = precond_dev(c, o, r, p, 1);
     if (st) return st;
-    k_dot<<<gr, bl, 0, c->stream>>>(g, r, p, c->partials, c->counters + 2, c->state, RD_RHO, 1);
+    launch(c, k_dot, gr, bl, g, r, p, c->partials, c->counters + 2, c->state, RD_RHO, 1);
     st = check_launch(c, "pcg init");
     if (st) return st;
     if (o->max_iter == 0) {
@@ -620,15 +620,15 @@ les_status pcg_fp64(les_ctx* c, const les_pcg_opts* o, les_pcg_result* res, int 
     int launched = 0, batch = 4;
     for (;;) {
         for (int it = 0; it < batch; ++it) {
-            k_spmv<<<gr, bl, 0, c->stream>>>(g, A, p, q, c->partials, c->counters + 1, c->state, DOT_ALPHA);
-            k_update<<<gr, bl, 0, c->stream>>>(g, A, x, r, p, q, z, c->partials, c->counters + 5, c->state,
+            launch_p(c, PROF_SPMV64, k_spmv, gr, bl, g, A, p, q, c->partials, c->counters + 1, c->state, DOT_ALPHA);
+            launch_p(c, PROF_UPDATE64, k_update, gr, bl, g, A, x, r, p, q, z, c->partials, c->counters + 5, c->state,
                                                 jac ? 1 : 0);
             if (!jac) {
                 st = precond_dev(c, o, r, z, 1);
                 if (st) return st;
-                k_dot<<<gr, bl, 0, c->stream>>>(g, r, z, c->partials, c->counters + 2, c->state, RD_BETA, 1);
+                launch(c, k_dot, gr, bl, g, r, z, c->partials, c->counters + 2, c->state, RD_BETA, 1);
             }
-            k_pupdate<<<gr, bl, 0, c->stream>>>(g, z, p, c->state);
+            launch(c, k_pupdate, gr, bl, g, z, p, c->state);
         }
         launched += batch;
         st = check_launch(c, "pcg iteration");
@@ -661,21 +661,21 @@ les_status solve_jacobi_dev(les_ctx* c, double dt, double rho, int max_iter, dou
     double* bufs[2] = {c->slot[LES_P], c->w[1]};
     const double dx2 = m.dx * m.dx, dy2 = m.dy * m.dy, dz2 = m.dz * m.dz;
     const double denom = 2 * (1.0 / dx2 + 1.0 / dy2 + 1.0 / dz2);
-    k_stat_rhs<<<gr, bl, 0, c->stream>>>(g, rho / dt, 2 * m.dx, 2 * m.dy, 2 * m.dz, c->slot[LES_U],
+    launch(c, k_stat_rhs, gr, bl, g, rho / dt, 2 * m.dx, 2 * m.dy, 2 * m.dz, c->slot[LES_U],
                                          c->slot[LES_V], c->slot[LES_W], rhs);
-    k_init_state<<<1, 1, 0, c->stream>>>(c->state, tol, max_iter, 0);
+    launch(c, k_init_state, 1, 1, c->state, tol, max_iter, 0);
     int launched = 0, batch = 8;
     int cur = 0;
     for (;;) {
         for (int it = 0; it < batch && launched < max_iter; ++it, ++launched) {
-            k_jacobi_sweep<<<gr, bl, 0, c->stream>>>(g, dx2, dy2, dz2, denom, bufs[cur], bufs[cur ^ 1], rhs,
+            launch(c, k_jacobi_sweep, gr, bl, g, dx2, dy2, dz2, denom, bufs[cur], bufs[cur ^ 1], rhs,
                                                      c->partials, c->counters + 6, c->state);
             cur ^= 1;
-            k_pbc_faces_guarded<<<gr, bl, 0, c->stream>>>(g, bufs[cur], bufs[cur], c->state);
+            launch(c, k_pbc_faces_guarded, gr, bl, g, bufs[cur], bufs[cur], c->state);
             if (c->n_solid)
-                k_pbc_obstacle_guarded<<<(c->n_solid + 255) / 256, 256, 0, c->stream>>>(
+                launch(c, k_pbc_obstacle_guarded, (c->n_solid + 255) / 256, 256, 
                     g, c->solid_list, c->n_solid, c->mask, bufs[cur], c->state);
-            k_stat_check<<<1, 1, 0, c->stream>>>(c->state, cur);
+            launch(c, k_stat_check, 1, 1, c->state, cur);
         }
         st = check_launch(c, "jacobi sweeps");
         if (st) return st;
@@ -703,7 +703,7 @@ les_status les_divergence(les_ctx* c, double dt, double rho)
     if (!c) return LES_BAD_ARG;
     cudaSetDevice(c->device);
     const les_mesh& m = c->mesh;
-    k_div_b<<<cell_grid(c->g), cell_block(), 0, c->stream>>>(
+    launch(c, k_div_b, cell_grid(c->g), cell_block(), 
         c->g, rho / dt, 1.0 / (2.0 * m.dx), 1.0 / (2.0 * m.dy), 1.0 / (2.0 * m.dz), 1.0 / m.dx,
         1.0 / m.dy, 1.0 / m.dz, c->slot[LES_U_NEW], c->slot[LES_V_NEW], c->slot[LES_W_NEW], c->mask,
         c->slot[LES_P_RHS], nullptr, c->partials, c->counters + 3, c->state, 0.0);
@@ -714,7 +714,7 @@ les_status les_build_b(les_ctx* c)
 {
     if (!c) return LES_BAD_ARG;
     cudaSetDevice(c->device);
-    k_build_b<<<cell_grid(c->g), cell_block(), 0, c->stream>>>(c->g, c->slot[LES_P_RHS], c->mask,
+    launch(c, k_build_b, cell_grid(c->g), cell_block(), c->g, c->slot[LES_P_RHS], c->mask,
                                                                 c->slot[LES_B]);
     return check_launch(c, "build b");
 }
@@ -741,7 +741,7 @@ les_status les_build_stencil(les_ctx* c)
     c->coef.x1 = -idx2; c->coef.x2 = -idx2 + -idx2;
     c->coef.y1 = -idy2; c->coef.y2 = -idy2 + -idy2;
     c->coef.z1 = -idz2; c->coef.z2 = -idz2 + -idz2;
-    k_build_code<<<cell_grid(c->g), cell_block(), 0, c->stream>>>(c->g, c->mask, c->code);
+    launch(c, k_build_code, cell_grid(c->g), cell_block(), c->g, c->mask, c->code);
     c->stencil_mode = 1;
     c->A_valid = false;   // a stale expansion of an older matrix must not be used
     return check_launch(c, "build stencil");
@@ -760,7 +760,7 @@ les_status les_get_stencil(les_ctx* c, double* const* diag7)
         st = check_cuda(c, cudaMalloc(&tmp[q], nb), "cudaMalloc(tmp)");
         if (st) return st;
     }
-    k_expand_stencil<<<cell_grid(c->g), cell_block(), 0, c->stream>>>(c->g, stencil_view(c), tmp[0], tmp[1],
+    launch(c, k_expand_stencil, cell_grid(c->g), cell_block(), c->g, stencil_view(c), tmp[0], tmp[1],
                                                                        tmp[2], tmp[3], tmp[4], tmp[5], tmp[6]);
     for (int q = 0; q < 7; ++q)
         if (diag7[q]) cudaMemcpyAsync(diag7[q], tmp[q], nb, cudaMemcpyDeviceToHost, c->stream);
@@ -835,14 +835,14 @@ les_status les_lambda_max(les_ctx* c, int n_iter, const double* v0, double* lamb
     StencilView A = stencil_view(c);
     double lam = 0.0;
     for (int it = 0; it < n_iter; ++it) {
-        k_spmv<<<gr, bl, 0, c->stream>>>(g, A, v, w, c->partials, c->counters + 1, c->state, DOT_SCAL0);
+        launch(c, k_spmv, gr, bl, g, A, v, w, c->partials, c->counters + 1, c->state, DOT_SCAL0);
         // lambda = v.w (spmv's fused dot is p.q = v.w)
         st = read_state(c);
         if (st) return st;
         lam = c->h_state->scal[0];
-        k_dot<<<gr, bl, 0, c->stream>>>(g, w, w, c->partials, c->counters + 2, c->state, RD_SCAL0, 0);
-        k_norm_of<<<1, 1, 0, c->stream>>>(c->state);
-        k_scale_inv<<<gr, bl, 0, c->stream>>>(g, v, w, c->state);   // v = w / ||w||
+        launch(c, k_dot, gr, bl, g, w, w, c->partials, c->counters + 2, c->state, RD_SCAL0, 0);
+        launch(c, k_norm_of, 1, 1, c->state);
+        launch(c, k_scale_inv, gr, bl, g, v, w, c->state);   // v = w / ||w||
         st = check_launch(c, "lambda iteration");
         if (st) return st;
     }

@@ -222,7 +222,7 @@ __global__ void k_stat_rhs_gs(Plane P, double coef, double two_dx, double two_dy
 
 Plane plane_of(const Geo& g) { return Plane{g.nx, g.ny, g.nz, g.si, g.sj}; }
 
-les_status coop_launch(les_ctx* c, const void* fn, void** args, int* grid_out)
+les_status coop_launch(les_ctx* c, const void* fn, void** args, int* grid_out, int pid = -1)
 {
     int per_sm = 0;
     les_status st = check_cuda(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, 0), "occupancy");
@@ -232,8 +232,13 @@ les_status coop_launch(les_ctx* c, const void* fn, void** args, int* grid_out)
     if (grid_out) *grid_out = grid;
     st = check_cuda(c, cudaMemsetAsync(c->gsync, 0, sizeof(unsigned) * 4, c->stream), "reset barrier");
     if (st) return st;
-    return check_cuda(c, cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, c->stream),
-                      "cooperative launch");
+    cudaEvent_t e1 = nullptr;
+    if (pid >= 0 && c->prof_on) prof_begin(c, pid, &e1);
+    st = check_cuda(c, cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, c->stream),
+                    "cooperative launch");
+    ++c->launches;
+    if (e1) cudaEventRecord(e1, c->stream);
+    return st;
 }
 
 GridSync grid_sync(les_ctx* c, int grid)
@@ -271,7 +276,7 @@ les_status ic_apply_dev(les_ctx* c, const double* r, double* z, const double* co
     const SolverState* stp = c->state;
     int skip = skip_done;
     void* args[] = {&P, (void*)&Lc, (void*)&Lw, (void*)&Ls, (void*)&Lb, (void*)&r, (void*)&z, &gs, (void*)&stp, &skip};
-    return coop_launch(c, (const void*)k_ic_apply<double>, args, nullptr);
+    return coop_launch(c, (const void*)k_ic_apply<double>, args, nullptr, PROF_IC);
 }
 
 les_status ic_apply_dev32(les_ctx* c, const float* r, float* z, const float* const* L, SolverState* st)
@@ -282,7 +287,7 @@ les_status ic_apply_dev32(les_ctx* c, const float* r, float* z, const float* con
     const SolverState* stp = st;
     int skip = st ? 1 : 0;
     void* args[] = {&P, (void*)&Lc, (void*)&Lw, (void*)&Ls, (void*)&Lb, (void*)&r, (void*)&z, &gs, (void*)&stp, &skip};
-    return coop_launch(c, (const void*)k_ic_apply<float>, args, nullptr);
+    return coop_launch(c, (const void*)k_ic_apply<float>, args, nullptr, PROF_IC);
 }
 
 les_status build_ic_dev(les_ctx* c)
@@ -318,7 +323,7 @@ les_status solve_gs_dev(les_ctx* c, double dt, double rho, int max_iter, double 
     // one slot per block of the cooperative grid (partials holds >= 4096)
     double* block_max = c->partials;
     if ((size_t)c->sms > c->partials_len) return fail(c, LES_BAD_ARG, "internal: partials too small");
-    k_stat_rhs_gs<<<(c->g.n + 255) / 256, 256, 0, c->stream>>>(P, rho / dt, 2 * m.dx, 2 * m.dy, 2 * m.dz,
+    launch(c, k_stat_rhs_gs, (c->g.n + 255) / 256, 256, P, rho / dt, 2 * m.dx, 2 * m.dy, 2 * m.dz,
                                                                c->slot[LES_U], c->slot[LES_V], c->slot[LES_W],
                                                                rhs, c->g.n);
     st = check_launch(c, "gs rhs");

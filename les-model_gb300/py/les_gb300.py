@@ -324,3 +324,35 @@ class Context:
         s = StepStats()
         self._chk(self.lib.les_step(self.h, C.byref(params), C.byref(s)))
         return s
+
+    # --- accounting
+    def mark(self, slot):
+        self._chk(self.lib.les_mark(self.h, int(slot)))
+
+    def elapsed(self, m0, m1):
+        ms = C.c_double()
+        self._chk(self.lib.les_elapsed(self.h, int(m0), int(m1), C.byref(ms)))
+        return ms.value
+
+    def launch_count(self):
+        self.lib.les_launch_count.restype = C.c_ulonglong
+        self.lib.les_launch_count.argtypes = [C.c_void_p]
+        return int(self.lib.les_launch_count(self.h))
+
+    def profile(self, enable):
+        self._chk(self.lib.les_profile(self.h, int(enable)))
+
+    def profile_read(self, kernel_id):
+        n = C.c_int()
+        ms = C.c_double()
+        self._chk(self.lib.les_profile_read(self.h, int(kernel_id), C.byref(n), C.byref(ms)))
+        return n.value, ms.value
+
+    def profile_all(self):
+        self.lib.les_profile_name.restype = C.c_char_p
+        out = {}
+        for kid in range(8):
+            n, ms = self.profile_read(kid)
+            if n:
+                out[self.lib.les_profile_name(kid).decode()] = (n, ms)
+        return out
