@@ -200,6 +200,9 @@ les_status les_spmv(les_ctx* ctx, int in_slot, int out_slot);
 les_status les_precond_apply(les_ctx* ctx, const les_pcg_opts* opts, int in_slot, int out_slot);
 /* parallel_dot, src/pressure.cpp:962-970. */
 les_status les_dot(les_ctx* ctx, int a_slot, int b_slot, double* out);
+/* out = a*in1 + b*in2: parallel_saxpy (src/pressure.cpp:995-1002), and
+ * parallel_axpy (:983-989) with a = 1, in1 = out.  Slots may alias. */
+les_status les_axpby(les_ctx* ctx, int out_slot, double a, int in1_slot, double b, int in2_slot);
 
 /* ---- accounting (no reference counterpart) ------------------------------ */
 /* Number of kernels this context has launched so far. */

@@ -40,6 +40,7 @@ def nvcc():
 def _deps():
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
     files.append(os.path.join(ROOT, "include", "les_gb300.h"))
+    files += [os.path.join(HERE, "host", f) for f in os.listdir(os.path.join(HERE, "host"))]
     return files
 
 
@@ -76,7 +77,25 @@ def build(force=False, verbose=False, extra=()):
         sys.stderr.write(" ".join(cmd) + "\n" + p.stdout + p.stderr)
         raise RuntimeError("link failed")
     os.replace(tmp, LIB)
+    build_shim()
     return LIB
+
+
+SHIM = os.path.join(HERE, "libles_shim.so")
+
+
+def build_shim():
+    """The reference-API shim (host/les_shim.cpp) over libles_gb300.so."""
+    tmp = SHIM + ".tmp%d" % os.getpid()
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-Wall", "-I", os.path.join(ROOT, "include"),
+           "-I", os.path.join(HERE, "host"), os.path.join(HERE, "host", "les_shim.cpp"), "-L", HERE,
+           "-lles_gb300", "-Wl,-rpath,$ORIGIN", "-o", tmp]
+    p = subprocess.run(cmd, capture_output=True, text=True)
+    if p.returncode:
+        sys.stderr.write(" ".join(cmd) + "\n" + p.stdout + p.stderr)
+        raise RuntimeError("shim build failed")
+    os.replace(tmp, SHIM)
+    return SHIM
 
 
 if __name__ == "__main__":

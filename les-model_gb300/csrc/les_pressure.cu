@@ -260,6 +260,16 @@ __global__ void k_dot(Geo g, const double* __restrict__ a, const double* __restr
 }
 
 // p = 1.0*z + beta*p (src/pressure.cpp:405).
+// out = a*in1 + b*in2 (parallel_saxpy, src/pressure.cpp:995-1002; with
+// a = 1, in1 = out it is parallel_axpy, :983-989).  out may alias either input.
+__global__ void k_axpby(Geo g, double a, const double* in1, double b, const double* in2, double* out)
+{
+    int i, j, k;
+    if (!cell_coords(g, i, j, k)) return;
+    const int id = i * g.si + j * g.sj + k;
+    out[id] = a * in1[id] + b * in2[id];
+}
+
 __global__ void k_pupdate(Geo g, const double* __restrict__ z, double* __restrict__ p, SolverState* st)
 {
     if (st->done) return;
@@ -783,11 +793,21 @@ les_status les_dot(les_ctx* c, int a, int b, double* out)
     return dot_dev(c, c->slot[a], c->slot[b], out);
 }
 
+les_status les_axpby(les_ctx* c, int out, double a, int in1, double b, int in2)
+{
+    if (!c || out < 0 || out >= LES_NSLOTS || in1 < 0 || in1 >= LES_NSLOTS || in2 < 0 || in2 >= LES_NSLOTS)
+        return LES_BAD_ARG;
+    cudaSetDevice(c->device);
+    launch(c, k_axpby, cell_grid(c->g), cell_block(), c->g, a, (const double*)c->slot[in1], b,
+           (const double*)c->slot[in2], c->slot[out]);
+    return check_launch(c, "axpby");
+}
+
 les_status les_precond_apply(les_ctx* c, const les_pcg_opts* o, int in, int out)
 {
     if (!c || !o || in < 0 || in >= LES_NSLOTS || out < 0 || out >= LES_NSLOTS || in == out) return LES_BAD_ARG;
     cudaSetDevice(c->device);
-    if (!c->stencil_mode) return fail(c, LES_BAD_ARG, "no matrix");
+    if (!c->stencil_mode && o->precond != LES_PC_IC) return fail(c, LES_BAD_ARG, "no matrix");
     if (o->precond == LES_PC_IC_A) {
         les_status st = ensure_stored_A(c);
         if (st) return st;
