@@ -204,6 +204,14 @@ les_status les_dot(les_ctx* ctx, int a_slot, int b_slot, double* out);
  * parallel_axpy (:983-989) with a = 1, in1 = out.  Slots may alias. */
 les_status les_axpby(les_ctx* ctx, int out_slot, double a, int in1_slot, double b, int in2_slot);
 
+/* ---- options (no reference counterpart) --------------------------------- */
+typedef enum les_option {
+    LES_OPT_FUSED = 0   /* 1 (default): mixed-precision inner iteration as two fused
+                           passes (Jacobi, Chebyshev degree 2..7); 0: one kernel per
+                           vector operation */
+} les_option;
+les_status les_set_option(les_ctx* ctx, int option, int value);
+
 /* ---- accounting (no reference counterpart) ------------------------------ */
 /* Number of kernels this context has launched so far. */
 unsigned long long les_launch_count(const les_ctx* ctx);

@@ -26,6 +26,7 @@ UNITS = {
     "les_pressure.cu": ["-fmad=false"],
     "les_wavefront.cu": ["-fmad=false"],
     "les_mixed.cu": [],
+    "les_fused.cu": [],
     "les_step.cu": ["-fmad=false"],
 }
 

@@ -331,6 +331,15 @@ les_status les_set_ic_factor(les_ctx* c, const double* const* diag7)
 
 unsigned long long les_launch_count(const les_ctx* c) { return c ? c->launches : 0ull; }
 
+les_status les_set_option(les_ctx* c, int option, int value)
+{
+    if (!c) return LES_BAD_ARG;
+    switch (option) {
+    case LES_OPT_FUSED: c->fused = value ? 1 : 0; return LES_OK;
+    default: return fail(c, LES_BAD_ARG, "unknown option");
+    }
+}
+
 les_status les_mark(les_ctx* c, int mark)
 {
     if (!c || mark < 0 || mark >= 64) return LES_BAD_ARG;

@@ -262,6 +262,7 @@ struct les_ctx {
     uint8_t* code = nullptr;
     double* A[7] = {};
     bool A_valid = false;         // A[] holds the current matrix (stored, or expanded codes)
+    int fused = 1;                // LES_OPT_FUSED: fused FP32 inner passes
     les::StencilCoef coef{};
     double* L[7] = {};
     bool have_L = false;

@@ -23,6 +23,7 @@
 #include <utility>
 
 #include "les_internal.cuh"
+#include "les_mixed.cuh"
 
 using namespace les;
 
@@ -41,42 +42,6 @@ __device__ __forceinline__ bool cell_coords(const Geo& g, int& i, int& j, int& k
     return k < g.nz && j < g.ny;
 }
 
-struct CoefF {
-    float c, w, e, s, n, b, t;
-};
-
-__device__ __forceinline__ float self(unsigned m, float v1, float v2) { return m == 0u ? 0.f : (m == 1u ? v1 : v2); }
-
-struct ViewF {
-    const uint8_t* code;
-    StencilCoefF k;
-    const float* d[7];   // stored mode: c, n, s, e, w, t, b
-    __device__ __forceinline__ CoefF at(int id) const
-    {
-        CoefF a;
-        if (code) {
-            unsigned cd = code[id];
-            if (cd == 0u) { a.c = 1.f; a.w = a.e = a.s = a.n = a.b = a.t = 0.f; return a; }
-            unsigned c = cd - 1u, xs = c % 5u, r = c / 5u, ys = r & 3u, zs = r >> 2;
-            a.c = k.c0;
-            a.w = self((XW_PACK >> (2 * xs)) & 3u, k.x1, k.x2);
-            a.e = self((XE_PACK >> (2 * xs)) & 3u, k.x1, k.x2);
-            a.s = self((YL_PACK >> (2 * ys)) & 3u, k.y1, k.y2);
-            a.n = self((YH_PACK >> (2 * ys)) & 3u, k.y1, k.y2);
-            a.b = self((YL_PACK >> (2 * zs)) & 3u, k.z1, k.z2);
-            a.t = self((YH_PACK >> (2 * zs)) & 3u, k.z1, k.z2);
-            return a;
-        }
-        a.c = d[0][id]; a.n = d[1][id]; a.s = d[2][id]; a.e = d[3][id];
-        a.w = d[4][id]; a.t = d[5][id]; a.b = d[6][id];
-        return a;
-    }
-    __device__ __forceinline__ float inv_diag(int id) const
-    {
-        if (code) return code[id] == 0 ? 1.f : 1.f / k.c0;
-        return 1.f / d[0][id];
-    }
-};
 
 __device__ __forceinline__ double row64(const StencilView& A, const double* __restrict__ x, const Geo& g,
                                         int i, int j, int k, int id)
@@ -438,7 +403,10 @@ les_status pcg_mixed_impl(les_ctx* c, const les_pcg_opts* o, les_pcg_result* res
     while (!c->h_state[0].done && outer < max_outer && c->h_state[0].iters < o->max_iter) {
         // ---- inner FP32 PCG on A e = r, e0 = 0
         launch(c, k_inner_init, 1, 1, in, out, o->inner_rtol, inner_cap);
-        if (mode == 2) {
+        if (c->fused && fused_supported(o)) {
+            st = inner_solve_fused(c, o, A32, in, out, inner_cap);
+            if (st) return st;
+        } else if (mode == 2) {
             launch(c, k_zero_f, gr, bl, g, e);
             st = inner_precond(c, o, A32, r, z, in, L32, 0, 1);
         } else {
@@ -450,7 +418,7 @@ les_status pcg_mixed_impl(les_ctx* c, const les_pcg_opts* o, les_pcg_result* res
         }
         if (st) return st;
         int cur = 0, launched = 0, batch = 4;
-        for (;;) {
+        for (; !(c->fused && fused_supported(o));) {   // unfused kernels (IC; fused path off)
             for (int it = 0; it < batch; ++it) {
                 launch_p(c, PROF_IN_SPMV, k_in_spmv, gr, bl, g, A32, z, pb[cur], pb[cur ^ 1], q, launched + it == 0 ? 1 : 0,
                                                     c->partials, c->counters + 10, in);

@@ -24,6 +24,7 @@ SLOTS = {"u": U, "v": V, "w": W, "u_new": U_NEW, "v_new": V_NEW, "w_new": W_NEW,
 SOLVER_PCG, SOLVER_JACOBI, SOLVER_GS = 0, 1, 2
 PC_JACOBI, PC_IC, PC_CHEBYSHEV, PC_IC_A = 0, 1, 2, 3
 FP64, MIXED = 0, 1
+OPT_FUSED = 0
 DIAGS = ("c", "n", "s", "e", "w", "t", "b")
 
 _dp = C.POINTER(C.c_double)
@@ -324,6 +325,9 @@ class Context:
         s = StepStats()
         self._chk(self.lib.les_step(self.h, C.byref(params), C.byref(s)))
         return s
+
+    def set_option(self, option, value):
+        self._chk(self.lib.les_set_option(self.h, int(option), int(value)))
 
     # --- accounting
     def mark(self, slot):

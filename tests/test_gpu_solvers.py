@@ -164,3 +164,54 @@ def test_mixed_ic_stalls_like_fp64():
     assert st64 == G.NOT_CONVERGED and st32 == G.NOT_CONVERGED
     assert np.isfinite(r32.residual) and np.all(np.isfinite(x32))
     assert r32.residual <= 10 * r64.residual
+
+
+def _odd_system(shape, seed):
+    """A random-obstacle system on an odd grid (partial tiles and chunks)."""
+    rng = np.random.default_rng(seed)
+    n = int(np.prod(shape))
+    h = 1.0 / 32
+    m = G.Mesh(*shape, h, h, h)
+    solid = (rng.random(n) < 0.05).astype(np.uint8)
+    f = les_cases.init_fields(shape, 0.05, seed)
+    with G.Context(m) as c:
+        c.upload_mask(np.zeros(n, np.uint8))
+        c.build_stencil()
+        lmax = c.lambda_max(20)
+        c.upload_fields(f)
+        c.upload_mask(solid)
+        c.sgs_nut(les_cases.CS)
+        c.momentum(1e-4, les_cases.NU)
+        c.velocity_bcs()
+        c.divergence(1e-4, les_cases.RHO)
+        c.build_b()
+        b = c.download("b")
+    return m, b, lmax
+
+
+@pytest.mark.parametrize("shape", [(45, 37, 70), (70, 19, 33)], ids=["45x37x70", "70x19x33"])
+@pytest.mark.parametrize("pc,deg", [(G.PC_CHEBYSHEV, 2), (G.PC_CHEBYSHEV, 4), (G.PC_CHEBYSHEV, 5),
+                                    (G.PC_JACOBI, 0)], ids=["cheb2", "cheb4", "cheb5", "jacobi"])
+def test_fused_inner_matches_unfused(shape, pc, deg):
+    """The fused two-pass FP32 inner iteration (temporally blocked Chebyshev)
+    follows the same iteration as the one-kernel-per-operation path: same
+    outer sweeps, inner counts within 2%, pressure within the mixed-vs-FP64
+    bar (1e-6 relative)."""
+    m, b, lmax = _odd_system(shape, sum(shape) + deg)
+    tol = 1e-8 * np.linalg.norm(b)
+    res = {}
+    for fused in (1, 0):
+        with G.Context(m) as c:
+            c.set_option(G.OPT_FUSED, fused)
+            c.upload_mask(np.zeros(m.n, np.uint8))
+            c.build_stencil()
+            c.upload("b", b)
+            c.upload("p", np.zeros(m.n))
+            st, r = c.pcg(G.pcg_opts(precond=pc, max_iter=20000, tol=tol, lambda_min=3 * np.pi ** 2,
+                                     lambda_max=lmax, degree=max(deg, 1), precision=G.MIXED, inner_rtol=1e-4))
+            res[fused] = (st, r.iters, r.outer, r.residual, c.download("p"))
+    (s1, i1, o1, r1, x1), (s0, i0, o0, r0, x0) = res[1], res[0]
+    assert s1 == G.OK and s0 == G.OK, (res[1][:4], res[0][:4])
+    assert r1 < tol and r0 < tol
+    assert abs(i1 - i0) <= max(2, 0.02 * i0), (i1, i0)
+    assert maxrel(x1, x0) < 1e-6, maxrel(x1, x0)
