@@ -125,12 +125,11 @@ class Clocks:
 
 # algorithmic HBM bytes per cell of one launch of each profiled kernel
 def alg_bytes_per_cell(name, degree):
-    if name == "inner_cheb_f32":
-        # zin, r, code, pout, zout (+ pin after the first step of each apply)
-        steps = max(degree - 1, 1)
-        return (17.0 + 21.0 * (steps - 1)) / steps
-    return {"inner_spmv_f32": 17.0, "inner_update_f32": 28.0, "spmv_f64": 17.0, "update_f64": 48.0,
-            "cheb_f64": 41.0, "outer_resid_f64": 21.0}.get(name)
+    # fused FP32 inner passes (the default): pass B reads r, q, p, e and the
+    # stencil code and writes r', e', z (the whole Chebyshev apply happens in
+    # shared memory); pass A reads z, p_old and the code and writes p, q
+    return {"inner_precond_f32": 29.0, "inner_spmv_f32": 17.0, "inner_update_f32": 28.0, "spmv_f64": 17.0,
+            "update_f64": 48.0, "cheb_f64": 41.0, "outer_resid_f64": 21.0}.get(name)
 
 
 def pc_code(G, name):

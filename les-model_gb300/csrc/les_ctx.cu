@@ -400,7 +400,7 @@ les_status les_profile_read(les_ctx* c, int kernel_id, int* launches, double* to
 
 const char* les_profile_name(int kernel_id)
 {
-    static const char* names[PROF_N] = {"inner_cheb_f32", "inner_spmv_f32", "inner_update_f32", "spmv_f64",
+    static const char* names[PROF_N] = {"inner_precond_f32", "inner_spmv_f32", "inner_update_f32", "spmv_f64",
                                         "update_f64",     "cheb_f64",       "outer_resid_f64",  "ic_apply"};
     return (kernel_id >= 0 && kernel_id < PROF_N) ? names[kernel_id] : "unknown";
 }

@@ -96,15 +96,21 @@ __global__ void __launch_bounds__(NT) k_pass_a(Geo g, ViewF A, int CI, const flo
         if (own && C >= i0 && C < i1) {
             const float* cb = sp[C % 3];
             const int id = C * g.si + gj * g.sj + gk;
-            CoefF a = A.at(id);
             const float pc = cb[opt];
-            float val = a.c * pc;
-            if (C > 0) val += a.w * sp[(C + 2) % 3][opt];
-            if (C < g.nx - 1) val += a.e * sp[(C + 1) % 3][opt];
-            if (gj > 0) val += a.s * cb[opt - W];
-            if (gj < g.ny - 1) val += a.n * cb[opt + W];
-            if (gk > 0) val += a.b * cb[opt - 1];
-            if (gk < g.nz - 1) val += a.t * cb[opt + 1];
+            float val;
+            if (A.interior(id)) {
+                val = A.k.c0 * pc + A.k.x1 * (sp[(C + 2) % 3][opt] + sp[(C + 1) % 3][opt]) +
+                      A.k.y1 * (cb[opt - W] + cb[opt + W]) + A.k.z1 * (cb[opt - 1] + cb[opt + 1]);
+            } else {
+                CoefF a = A.at(id);
+                val = a.c * pc;
+                if (C > 0) val += a.w * sp[(C + 2) % 3][opt];
+                if (C < g.nx - 1) val += a.e * sp[(C + 1) % 3][opt];
+                if (gj > 0) val += a.s * cb[opt - W];
+                if (gj < g.ny - 1) val += a.n * cb[opt + W];
+                if (gk > 0) val += a.b * cb[opt - 1];
+                if (gk < g.nz - 1) val += a.t * cb[opt + 1];
+            }
             q[id] = val;
             acc_prod(acc, pc, val);
         }
@@ -195,15 +201,21 @@ __global__ void __launch_bounds__(NT) k_pass_b(Geo g, ViewF A, int CI, ChebF cf,
                     if (j < 0 || j >= g.ny || k < 0 || k >= g.nz) continue;
                     const int pt = jj * W + kk;
                     const int id = Pk * g.si + j * g.sj + k;
-                    CoefF a = A.at(id);
                     const float zcv = zc[pt];
-                    float az = a.c * zcv;
-                    if (Pk > 0) az += a.w * zw[pt];
-                    if (Pk < g.nx - 1) az += a.e * ze[pt];
-                    if (j > 0) az += a.s * zc[pt - W];
-                    if (j < g.ny - 1) az += a.n * zc[pt + W];
-                    if (k > 0) az += a.b * zc[pt - 1];
-                    if (k < g.nz - 1) az += a.t * zc[pt + 1];
+                    float az;
+                    if (A.interior(id)) {   // all six neighbours present, base coefficients
+                        az = A.k.c0 * zcv + A.k.x1 * (zw[pt] + ze[pt]) + A.k.y1 * (zc[pt - W] + zc[pt + W]) +
+                             A.k.z1 * (zc[pt - 1] + zc[pt + 1]);
+                    } else {
+                        CoefF a = A.at(id);
+                        az = a.c * zcv;
+                        if (Pk > 0) az += a.w * zw[pt];
+                        if (Pk < g.nx - 1) az += a.e * ze[pt];
+                        if (j > 0) az += a.s * zc[pt - W];
+                        if (j < g.ny - 1) az += a.n * zc[pt + W];
+                        if (k > 0) az += a.b * zc[pt - 1];
+                        if (k < g.nz - 1) az += a.t * zc[pt + 1];
+                    }
                     const float rv = rpl[pt];
                     const float res = rv - az;
                     const float pck = fmaf(cf.b[lv - 1], pcp[pt], res);
@@ -295,7 +307,32 @@ les_status inner_solve_fused(les_ctx* c, const les_pcg_opts* o, ViewF A, SolverS
     }
     float* r[2] = {c->f[0], c->f[6]};
     float *z = c->f[1], *pb[2] = {c->f[2], c->f[3]}, *q = c->f[4], *e = c->f[5];
-    const int CIA = 16, CIB = 32;
+    // chunk lengths along i chosen so that each pass fills about one wave of
+    // resident blocks (longer chunks amortise the i-halo of the march)
+    const int tiles = ((g.nz + TK - 1) / TK) * ((g.ny + TJ - 1) / TJ);
+    auto chunk = [&](const void* fn, size_t smem, int min_ci) {
+        int occ = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, NT, smem);
+        int chunks = (occ < 1 ? 1 : occ) * c->sms / tiles;
+        if (chunks < 1) chunks = 1;
+        int ci = (g.nx + chunks - 1) / chunks;
+        return ci < min_ci ? min_ci : ci;
+    };
+    size_t smem_b = 0;
+    const void* fb = nullptr;
+    switch (S) {
+    case 0: smem_b = BSmem<0>::BYTES; fb = (const void*)k_pass_b<0, false>; break;
+    case 1: smem_b = BSmem<1>::BYTES; fb = (const void*)k_pass_b<1, false>; break;
+    case 2: smem_b = BSmem<2>::BYTES; fb = (const void*)k_pass_b<2, false>; break;
+    case 3: smem_b = BSmem<3>::BYTES; fb = (const void*)k_pass_b<3, false>; break;
+    case 4: smem_b = BSmem<4>::BYTES; fb = (const void*)k_pass_b<4, false>; break;
+    case 5: smem_b = BSmem<5>::BYTES; fb = (const void*)k_pass_b<5, false>; break;
+    default: smem_b = BSmem<6>::BYTES; fb = (const void*)k_pass_b<6, false>; break;
+    }
+    if (smem_b > 48 * 1024)
+        cudaFuncSetAttribute(fb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b);
+    const int CIA = chunk((const void*)k_pass_a<false>, 0, 8);
+    const int CIB = chunk(fb, smem_b, 4 * S > 8 ? 4 * S : 8);
     const dim3 ga((g.nz + TK - 1) / TK, (g.ny + TJ - 1) / TJ, (g.nx + CIA - 1) / CIA);
     const dim3 gb((g.nz + TK - 1) / TK, (g.ny + TJ - 1) / TJ, (g.nx + CIB - 1) / CIB);
     auto pass_b = [&](bool first, const float* rin, float* rout, const float* p) -> les_status {

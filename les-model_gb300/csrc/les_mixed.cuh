@@ -19,11 +19,21 @@ struct ViewF {
     const uint8_t* code;
     StencilCoefF k;
     const float* d[7];   // stored mode: c, n, s, e, w, t, b
+    // Code 1 = all three axes in state 0: a fluid cell whose six neighbours
+    // all exist and are fluid, with the base coefficients.
+    __device__ __forceinline__ bool interior(int id) const { return code && code[id] == 1u; }
+    __device__ __forceinline__ CoefF base() const
+    {
+        CoefF a;
+        a.c = k.c0; a.w = a.e = k.x1; a.s = a.n = k.y1; a.b = a.t = k.z1;
+        return a;
+    }
     __device__ __forceinline__ CoefF at(int id) const
     {
         CoefF a;
         if (code) {
             unsigned cd = code[id];
+            if (cd == 1u) return base();
             if (cd == 0u) {
                 a.c = 1.f; a.w = a.e = a.s = a.n = a.b = a.t = 0.f;
                 return a;
