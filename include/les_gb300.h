@@ -204,6 +204,21 @@ les_status les_dot(les_ctx* ctx, int a_slot, int b_slot, double* out);
  * parallel_axpy (:983-989) with a = 1, in1 = out.  Slots may alias. */
 les_status les_axpby(les_ctx* ctx, int out_slot, double a, int in1_slot, double b, int in2_slot);
 
+/* Dot product of two device vectors that allocates nothing (no counterpart
+ * in the reference).  For callers that cannot call cudaMalloc -- code running
+ * under a memory pool or arena that owns the process's device allocations, or
+ * a thread that must not take the allocator's locks mid-step.  a, b: device
+ * arrays of n doubles; out: device pointer that receives the result; stream:
+ * a cudaStream_t (NULL for the default stream); the call is asynchronous on
+ * it.  Scratch is a fixed array reserved in device memory when the library is
+ * loaded (512 KiB on every device that loads it, held until exit), which caps
+ * n at LES_NOALLOC_MAX_CELLS; larger n is rejected with LES_BAD_ARG and a
+ * message on stderr.  The first call on a device looks up that array's
+ * address (once per device): make that first call before any stream capture.
+ * All calls share the scratch, so calls that overlap on the GPU race. */
+#define LES_NOALLOC_MAX_CELLS 134217728LL
+les_status les_dot_noalloc(const double* a, const double* b, long long n, double* out, void* stream);
+
 /* ---- options (no reference counterpart) --------------------------------- */
 typedef enum les_option {
     LES_OPT_FUSED = 0   /* 1 (default): mixed-precision inner iteration as two fused

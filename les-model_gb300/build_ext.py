@@ -28,6 +28,7 @@ UNITS = {
     "les_mixed.cu": [],
     "les_fused.cu": [],
     "les_step.cu": ["-fmad=false"],
+    "les_noalloc.cu": ["-fmad=false"],
 }
 
 
