@@ -7,14 +7,16 @@
 //   the recurrence of les-model src/pressure.cpp:871-905; Jacobi: r'/A_c),
 //   and r'.z -> beta, rho.  Convergence is tested on ||r'||.
 //
-// Both passes march along i (the slowest axis) over a 32(k) x 8(j) tile and a
-// chunk of planes.  Pass A keeps a ring of three (tile + 1 halo) planes of p in
-// shared memory.  Pass B is temporally blocked: at march step I it computes
-// level 0 (r') at plane I and Chebyshev level k at plane I-k, each level over
-// the tile grown by S-k halo cells, from rings of planes of the level below
-// held in shared memory; only r, q, p, e are read and r', e', z written, once
-// per cell.  That is 17 + 29 bytes per cell per inner iteration instead of the
-// 104 of five unfused kernels.
+// Both passes march along i (the slowest axis) over a tile of rows (j) and
+// columns (k) and a chunk of planes.  Shared-memory rows are exactly 32 cells
+// wide, one warp per row, so the tile's output width in k is 32 minus the
+// halo: 30 for pass A (halo 1), 32-2S for pass B (halo S).  Pass A keeps a
+// ring of three planes of p.  Pass B is temporally blocked: at march step I it
+// computes level 0 (r') at plane I and Chebyshev level k at plane I-k, each
+// level over the tile grown by S-k halo cells, from rings of planes of the
+// level below (and of the stencil codes) held in shared memory; only r, q, p,
+// e and the codes are read and r', e', z written, once per cell: 17 + 29 bytes
+// per cell per inner iteration instead of 104 for five unfused kernels.
 //
 // Inner products are accumulated per thread in compensated FP32 (TwoProd +
 // TwoSum, i.e. double-float, ~48-bit significand) and summed across threads
@@ -29,7 +31,9 @@ using namespace les;
 
 namespace {
 
-constexpr int TK = 32, TJ = 8, NT = TK * TJ;
+constexpr int NT = 256;   // 8 warps
+constexpr int NW = NT / 32;
+constexpr int W = 32;     // shared-memory row width
 
 // double-float accumulator: the sum is hi + lo
 struct Acc {
@@ -58,82 +62,105 @@ __device__ __forceinline__ double acc_value(const Acc& a) { return (double)a.hi 
 __device__ __forceinline__ int imin(int a, int b) { return a < b ? a : b; }
 __device__ __forceinline__ int imax(int a, int b) { return a > b ? a : b; }
 
+// 7-point product at a cell whose code is `cd`, with the centre value zc and
+// the six neighbours (read only where the reference's bounds tests allow).
+struct Nb {
+    float w, e, s, n, b, t;
+};
+
+// ---- pass A -----------------------------------------------------------------
+constexpr int A_TK = W - 2;       // 30 output columns
+constexpr int A_TJ = 14;          // output rows
+constexpr int A_H = A_TJ + 2;     // 16 rows with halo = 2 per warp
+constexpr int A_PL = W * A_H;
+
 template <bool FIRST>
 __global__ void __launch_bounds__(NT) k_pass_a(Geo g, ViewF A, int CI, const float* __restrict__ z,
                                                 const float* __restrict__ pold, float* __restrict__ pnew,
                                                 float* __restrict__ q, double* partials, unsigned* counter,
                                                 SolverState* st)
 {
-    constexpr int W = TK + 2, H = TJ + 2, PL = W * H;
-    __shared__ float sp[3][PL];
+    __shared__ float sp[3][A_PL];
     __shared__ double sm[32];
     if (st->done) return;
     const float beta = FIRST ? 0.f : (float)st->beta;
-    const int tk = threadIdx.x, tj = threadIdx.y, tid = tk + TK * tj;
-    const int k0 = blockIdx.x * TK, j0 = blockIdx.y * TJ;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int k0 = blockIdx.x * A_TK, j0 = blockIdx.y * A_TJ;
     const int i0 = blockIdx.z * CI, i1 = imin(g.nx, i0 + CI);
-    const int gj = j0 + tj, gk = k0 + tk;
-    const bool own = gj < g.ny && gk < g.nz;
-    const int opt = (tj + 1) * W + (tk + 1);
+    const int kg = k0 - 1 + lane;
+    const bool kin = kg >= 0 && kg < g.nz;
+    const bool kcen = lane >= 1 && lane <= A_TK && kg < g.nz;
     Acc acc;
     for (int P = i0 - 1; P <= i1; ++P) {
         if (P >= 0 && P < g.nx) {
             float* buf = sp[P % 3];
-            for (int pt = tid; pt < PL; pt += NT) {
-                const int jj = pt / W, kk = pt - jj * W;
-                const int j = j0 - 1 + jj, k = k0 - 1 + kk;
+#pragma unroll
+            for (int rr = 0; rr < A_H / NW; ++rr) {
+                const int row = warp + rr * NW;
+                const int j = j0 - 1 + row;
                 float v = 0.f;
-                if (j >= 0 && j < g.ny && k >= 0 && k < g.nz) {
-                    const int id = P * g.si + j * g.sj + k;
+                if (kin && j >= 0 && j < g.ny) {
+                    const int id = P * g.si + j * g.sj + kg;
                     v = FIRST ? z[id] : fmaf(beta, pold[id], z[id]);
-                    if (jj >= 1 && jj <= TJ && kk >= 1 && kk <= TK && P >= i0 && P < i1) pnew[id] = v;
+                    if (kcen && row >= 1 && row <= A_TJ && P >= i0 && P < i1) pnew[id] = v;
                 }
-                buf[pt] = v;
+                buf[row * W + lane] = v;
             }
         }
         __syncthreads();
         const int C = P - 1;
-        if (own && C >= i0 && C < i1) {
+        if (C >= i0 && C < i1 && kcen) {
             const float* cb = sp[C % 3];
-            const int id = C * g.si + gj * g.sj + gk;
-            const float pc = cb[opt];
-            float val;
-            if (A.interior(id)) {
-                val = A.k.c0 * pc + A.k.x1 * (sp[(C + 2) % 3][opt] + sp[(C + 1) % 3][opt]) +
-                      A.k.y1 * (cb[opt - W] + cb[opt + W]) + A.k.z1 * (cb[opt - 1] + cb[opt + 1]);
-            } else {
-                CoefF a = A.at(id);
-                val = a.c * pc;
-                if (C > 0) val += a.w * sp[(C + 2) % 3][opt];
-                if (C < g.nx - 1) val += a.e * sp[(C + 1) % 3][opt];
-                if (gj > 0) val += a.s * cb[opt - W];
-                if (gj < g.ny - 1) val += a.n * cb[opt + W];
-                if (gk > 0) val += a.b * cb[opt - 1];
-                if (gk < g.nz - 1) val += a.t * cb[opt + 1];
+            const float* cw = sp[(C + 2) % 3];
+            const float* ce = sp[(C + 1) % 3];
+            for (int row = 1 + warp; row <= A_TJ; row += NW) {
+                const int j = j0 - 1 + row;
+                if (j >= g.ny) break;
+                const int pt = row * W + lane;
+                const int id = C * g.si + j * g.sj + kg;
+                const float pc = cb[pt];
+                float val;
+                if (A.interior(id)) {
+                    val = A.k.c0 * pc + A.k.x1 * (cw[pt] + ce[pt]) + A.k.y1 * (cb[pt - W] + cb[pt + W]) +
+                          A.k.z1 * (cb[pt - 1] + cb[pt + 1]);
+                } else {
+                    CoefF a = A.at(id);
+                    val = a.c * pc;
+                    if (C > 0) val += a.w * cw[pt];
+                    if (C < g.nx - 1) val += a.e * ce[pt];
+                    if (j > 0) val += a.s * cb[pt - W];
+                    if (j < g.ny - 1) val += a.n * cb[pt + W];
+                    if (kg > 0) val += a.b * cb[pt - 1];
+                    if (kg < g.nz - 1) val += a.t * cb[pt + 1];
+                }
+                q[id] = val;
+                acc_prod(acc, pc, val);
             }
-            q[id] = val;
-            acc_prod(acc, pc, val);
         }
         __syncthreads();
     }
     double v[1] = {acc_value(acc)};
     if (last_block_sum<1>(v, partials, counter, sm)) {
-        if (tid == 0) st->alpha = st->rho / v[0];
+        if (threadIdx.x == 0) st->alpha = st->rho / v[0];
     }
 }
 
+// ---- pass B -----------------------------------------------------------------
 struct ChebF {
     float a0;
     float a[8], b[8];
 };
 
 template <int S>
-struct BSmem {
-    static constexpr int W = TK + 2 * S, H = TJ + 2 * S, PL = W * H;
+struct BGeom {
+    static constexpr int TK = W - 2 * S;   // output columns
+    static constexpr int TJ = 16;          // output rows
+    static constexpr int H = TJ + 2 * S;   // rows of the level-0 region
+    static constexpr int PL = W * H;       // cells per shared-memory plane
     // r' ring (S+1 planes), z_k rings (3 planes each, k = 0..S-1), pc_k rings
-    // (2 planes each, k = 1..S-1)
+    // (2 planes each, k = 1..S-1), then the stencil-code ring (S+1 planes)
     static constexpr int FLOATS = (S + 1) * PL + 3 * S * PL + 2 * (S > 1 ? S - 1 : 0) * PL;
-    static constexpr size_t BYTES = sizeof(float) * (size_t)FLOATS;
+    static constexpr size_t BYTES = sizeof(float) * (size_t)FLOATS + (size_t)(S + 1) * PL;
 };
 
 // S = 0: Jacobi (z = r'/A_c, no stencil levels).
@@ -144,34 +171,42 @@ __global__ void __launch_bounds__(NT) k_pass_b(Geo g, ViewF A, int CI, ChebF cf,
                                                 float* __restrict__ z_out, double* partials, unsigned* counter,
                                                 SolverState* st, SolverState* outer, int total_cap)
 {
-    using SM = BSmem<S>;
-    constexpr int W = SM::W, H = SM::H, PL = SM::PL;
+    using GB = BGeom<S>;
+    constexpr int TK = GB::TK, TJ = GB::TJ, H = GB::H, PL = GB::PL;
     extern __shared__ float dsm[];
     __shared__ double sm[64];
     if (st->done) return;
-    float* rp = dsm;                               // [(S+1)][PL]
-    float* zr = rp + (S + 1) * PL;                 // [S][3][PL]
-    float* pcr = zr + 3 * S * PL;                  // [S-1][2][PL]
+    float* rp = dsm;                                        // [(S+1)][PL]
+    float* zr = rp + (S + 1) * PL;                          // [S][3][PL]
+    float* pcr = zr + 3 * S * PL;                           // [S-1][2][PL]
+    uint8_t* cr = reinterpret_cast<uint8_t*>(dsm + GB::FLOATS);   // [(S+1)][PL]
     const float alpha = FIRST ? 0.f : (float)st->alpha;
-    const int tid = threadIdx.x + TK * threadIdx.y;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int k0 = blockIdx.x * TK, j0 = blockIdx.y * TJ;
     const int i0 = blockIdx.z * CI, i1 = imin(g.nx, i0 + CI);
+    const int kg = k0 - S + lane;                          // this lane's global k
+    const bool kin = kg >= 0 && kg < g.nz;
+    const bool kcen = lane >= S && lane < S + TK && kin;
     Acc arr, arz;
     for (int I = i0 - S; I < i1 + S; ++I) {
-        // ---- level 0 at plane I: r' = r - alpha q over tile + S halo
-        if (I >= 0 && I < g.nx && I < i1 + S) {
-            float* rpl = rp + (I % (S + 1)) * PL;
-            for (int pt = tid; pt < PL; pt += NT) {
-                const int jj = pt / W, kk = pt - jj * W;
-                const int j = j0 - S + jj, k = k0 - S + kk;
-                if (j < 0 || j >= g.ny || k < 0 || k >= g.nz) continue;
-                const int id = I * g.si + j * g.sj + k;
+        // ---- level 0 at plane I: r' = r - alpha q over the tile + S halo
+        if (I >= 0 && I < g.nx) {
+            const int slot = I % (S + 1);
+            float* rpl = rp + slot * PL;
+            uint8_t* crl = cr + slot * PL;
+            float* z0 = zr + (I % 3) * PL;
+            const bool plane_out = I >= i0 && I < i1;
+            for (int row = warp; row < H; row += NW) {
+                const int j = j0 - S + row;
+                const int pt = row * W + lane;
+                if (!kin || j < 0 || j >= g.ny) continue;
+                const int id = I * g.si + j * g.sj + kg;
                 const float rold = r_in[id];
                 const float rv = FIRST ? rold : fmaf(-alpha, q[id], rold);
                 rpl[pt] = rv;
-                const bool center = jj >= S && jj < S + TJ && kk >= S && kk < S + TK && I >= i0 && I < i1;
-                if (S > 0) zr[(I % 3) * PL + pt] = cf.a0 * rv;
-                if (center) {
+                crl[pt] = A.code ? A.code[id] : (uint8_t)2;
+                if (S > 0) z0[pt] = cf.a0 * rv;
+                if (plane_out && kcen && row >= S && row < S + TJ) {
                     r_out[id] = rv;
                     e[id] = FIRST ? 0.f : fmaf(alpha, p[id], e[id]);
                     acc_prod(arr, rv, rv);
@@ -184,47 +219,50 @@ __global__ void __launch_bounds__(NT) k_pass_b(Geo g, ViewF A, int CI, ChebF cf,
             }
         }
         __syncthreads();
-        // ---- Chebyshev levels k = 1..S at plane I-k
+        // ---- Chebyshev levels 1..S at plane I-lv over the tile + (S-lv) halo
 #pragma unroll
         for (int lv = 1; lv <= S; ++lv) {
             const int Pk = I - lv;
-            if (Pk >= imax(0, i0 - S + lv) && Pk < imin(g.nx, i1 + S - lv)) {
-                const int Wk = W - 2 * lv, Hk = H - 2 * lv, PLk = Wk * Hk;
+            if (Pk >= imax(0, i0 - S + lv) && Pk < imin(g.nx, i1 + S - lv) && kin && lane >= lv &&
+                lane < W - lv) {
                 const float* zc = zr + ((lv - 1) * 3 + Pk % 3) * PL;
                 const float* zw = zr + ((lv - 1) * 3 + (Pk + 2) % 3) * PL;
                 const float* ze = zr + ((lv - 1) * 3 + (Pk + 1) % 3) * PL;
                 const float* rpl = rp + (Pk % (S + 1)) * PL;
+                const uint8_t* crl = cr + (Pk % (S + 1)) * PL;
                 const float* pcp = lv >= 2 ? pcr + ((lv - 2) * 2 + Pk % 2) * PL : rpl;
-                for (int qq = tid; qq < PLk; qq += NT) {
-                    const int jj = lv + qq / Wk, kk = lv + qq % Wk;
-                    const int j = j0 - S + jj, k = k0 - S + kk;
-                    if (j < 0 || j >= g.ny || k < 0 || k >= g.nz) continue;
-                    const int pt = jj * W + kk;
-                    const int id = Pk * g.si + j * g.sj + k;
+                float* zo = lv < S ? zr + (lv * 3 + Pk % 3) * PL : nullptr;
+                float* po = lv < S ? pcr + ((lv - 1) * 2 + Pk % 2) * PL : nullptr;
+                const bool out_lane = lv == S && kcen && Pk >= i0 && Pk < i1;
+                for (int row = lv + warp; row < H - lv; row += NW) {
+                    const int j = j0 - S + row;
+                    if (j < 0 || j >= g.ny) continue;
+                    const int pt = row * W + lane;
+                    const unsigned cd = crl[pt];
                     const float zcv = zc[pt];
                     float az;
-                    if (A.interior(id)) {   // all six neighbours present, base coefficients
+                    if (cd == 1u) {   // all six neighbours present, base coefficients
                         az = A.k.c0 * zcv + A.k.x1 * (zw[pt] + ze[pt]) + A.k.y1 * (zc[pt - W] + zc[pt + W]) +
                              A.k.z1 * (zc[pt - 1] + zc[pt + 1]);
                     } else {
+                        const int id = Pk * g.si + j * g.sj + kg;
                         CoefF a = A.at(id);
                         az = a.c * zcv;
                         if (Pk > 0) az += a.w * zw[pt];
                         if (Pk < g.nx - 1) az += a.e * ze[pt];
                         if (j > 0) az += a.s * zc[pt - W];
                         if (j < g.ny - 1) az += a.n * zc[pt + W];
-                        if (k > 0) az += a.b * zc[pt - 1];
-                        if (k < g.nz - 1) az += a.t * zc[pt + 1];
+                        if (kg > 0) az += a.b * zc[pt - 1];
+                        if (kg < g.nz - 1) az += a.t * zc[pt + 1];
                     }
                     const float rv = rpl[pt];
-                    const float res = rv - az;
-                    const float pck = fmaf(cf.b[lv - 1], pcp[pt], res);
+                    const float pck = fmaf(cf.b[lv - 1], pcp[pt], rv - az);
                     const float zk = fmaf(cf.a[lv - 1], pck, zcv);
                     if (lv < S) {
-                        zr[(lv * 3 + Pk % 3) * PL + pt] = zk;
-                        pcr[((lv - 1) * 2 + Pk % 2) * PL + pt] = pck;
-                    } else if (jj >= S && jj < S + TJ && kk >= S && kk < S + TK && Pk >= i0 && Pk < i1) {
-                        z_out[id] = zk;
+                        zo[pt] = zk;
+                        po[pt] = pck;
+                    } else if (out_lane && row >= S && row < S + TJ) {
+                        z_out[Pk * g.si + j * g.sj + kg] = zk;
                         acc_prod(arz, rv, zk);
                     }
                 }
@@ -234,7 +272,7 @@ __global__ void __launch_bounds__(NT) k_pass_b(Geo g, ViewF A, int CI, ChebF cf,
     }
     double v[2] = {acc_value(arr), acc_value(arz)};
     if (last_block_sum<2>(v, partials, counter, sm)) {
-        if (tid == 0) {
+        if (threadIdx.x == 0) {
             if (FIRST) {
                 st->rho = v[1];
             } else {
@@ -255,24 +293,39 @@ __global__ void __launch_bounds__(NT) k_pass_b(Geo g, ViewF A, int CI, ChebF cf,
 }
 
 template <int S>
-les_status launch_b(les_ctx* c, bool first, dim3 gr, ViewF A, int CI, const ChebF& cf, const float* rin,
-                    float* rout, const float* q, const float* p, float* e, float* z, SolverState* in,
-                    SolverState* out, int cap)
+const void* pass_b_fn(bool first)
 {
-    const size_t bytes = BSmem<S>::BYTES;
+    return first ? (const void*)k_pass_b<S, true> : (const void*)k_pass_b<S, false>;
+}
+
+template <int S>
+les_status launch_b(les_ctx* c, bool first, int CI, ViewF A, const ChebF& cf, const float* rin, float* rout,
+                    const float* q, const float* p, float* e, float* z, SolverState* in, SolverState* out, int cap)
+{
+    const Geo& g = c->g;
+    const size_t bytes = BGeom<S>::BYTES;
+    const dim3 gr((g.nz + BGeom<S>::TK - 1) / BGeom<S>::TK, (g.ny + BGeom<S>::TJ - 1) / BGeom<S>::TJ,
+                  (g.nx + CI - 1) / CI);
     auto kf = first ? k_pass_b<S, true> : k_pass_b<S, false>;
-    if (bytes > 48 * 1024) {
-        les_status st = check_cuda(c, cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes),
-                                   "smem attribute");
-        if (st) return st;
-    }
     cudaEvent_t e1 = nullptr;
     if (c->prof_on) prof_begin(c, PROF_IN_CHEB, &e1);
-    kf<<<gr, dim3(TK, TJ), bytes, c->stream>>>(c->g, A, CI, cf, rin, rout, q, p, e, z, c->partials, c->counters + 14,
-                                               in, out, cap);
+    kf<<<gr, NT, bytes, c->stream>>>(g, A, CI, cf, rin, rout, q, p, e, z, c->partials, c->counters + 14, in, out,
+                                      cap);
     ++c->launches;
     if (e1) cudaEventRecord(e1, c->stream);
     return LES_OK;
+}
+
+// Chunk length along i so that a pass fills about one wave of resident
+// blocks (longer chunks amortise the i-halo of the march).
+int chunk_len(les_ctx* c, const void* fn, size_t smem, int tiles, int min_ci)
+{
+    int occ = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, NT, smem);
+    int chunks = (occ < 1 ? 1 : occ) * c->sms / (tiles < 1 ? 1 : tiles);
+    if (chunks < 1) chunks = 1;
+    int ci = (c->g.nx + chunks - 1) / chunks;
+    return ci < min_ci ? min_ci : ci;
 }
 
 }  // namespace
@@ -285,7 +338,7 @@ bool fused_supported(const les_pcg_opts* o)
     return o->precond == LES_PC_CHEBYSHEV && o->degree >= 2 && o->degree <= 7;
 }
 
-// One inner FP32 solve A e = r (e from 0) with the fused passes.  r0 holds
+// One inner FP32 solve A e = r (e from 0) with the fused passes.  f[0] holds
 // the right-hand side on entry and is used as scratch.
 les_status inner_solve_fused(les_ctx* c, const les_pcg_opts* o, ViewF A, SolverState* in, SolverState* out,
                              int inner_cap)
@@ -307,54 +360,47 @@ les_status inner_solve_fused(les_ctx* c, const les_pcg_opts* o, ViewF A, SolverS
     }
     float* r[2] = {c->f[0], c->f[6]};
     float *z = c->f[1], *pb[2] = {c->f[2], c->f[3]}, *q = c->f[4], *e = c->f[5];
-    // chunk lengths along i chosen so that each pass fills about one wave of
-    // resident blocks (longer chunks amortise the i-halo of the march)
-    const int tiles = ((g.nz + TK - 1) / TK) * ((g.ny + TJ - 1) / TJ);
-    auto chunk = [&](const void* fn, size_t smem, int min_ci) {
-        int occ = 1;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, NT, smem);
-        int chunks = (occ < 1 ? 1 : occ) * c->sms / tiles;
-        if (chunks < 1) chunks = 1;
-        int ci = (g.nx + chunks - 1) / chunks;
-        return ci < min_ci ? min_ci : ci;
-    };
+
     size_t smem_b = 0;
-    const void* fb = nullptr;
+    int tk_b = W, tj_b = 16;
+    const void* fb[2] = {};
     switch (S) {
-    case 0: smem_b = BSmem<0>::BYTES; fb = (const void*)k_pass_b<0, false>; break;
-    case 1: smem_b = BSmem<1>::BYTES; fb = (const void*)k_pass_b<1, false>; break;
-    case 2: smem_b = BSmem<2>::BYTES; fb = (const void*)k_pass_b<2, false>; break;
-    case 3: smem_b = BSmem<3>::BYTES; fb = (const void*)k_pass_b<3, false>; break;
-    case 4: smem_b = BSmem<4>::BYTES; fb = (const void*)k_pass_b<4, false>; break;
-    case 5: smem_b = BSmem<5>::BYTES; fb = (const void*)k_pass_b<5, false>; break;
-    default: smem_b = BSmem<6>::BYTES; fb = (const void*)k_pass_b<6, false>; break;
+#define LES_CASE(s)                                                          \
+    case s: smem_b = BGeom<s>::BYTES; tk_b = BGeom<s>::TK; tj_b = BGeom<s>::TJ; \
+        fb[0] = pass_b_fn<s>(true); fb[1] = pass_b_fn<s>(false); break;
+        LES_CASE(0) LES_CASE(1) LES_CASE(2) LES_CASE(3) LES_CASE(4) LES_CASE(5)
+    default: LES_CASE(6)
+#undef LES_CASE
     }
     if (smem_b > 48 * 1024)
-        cudaFuncSetAttribute(fb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b);
-    const int CIA = chunk((const void*)k_pass_a<false>, 0, 8);
-    const int CIB = chunk(fb, smem_b, 4 * S > 8 ? 4 * S : 8);
-    const dim3 ga((g.nz + TK - 1) / TK, (g.ny + TJ - 1) / TJ, (g.nx + CIA - 1) / CIA);
-    const dim3 gb((g.nz + TK - 1) / TK, (g.ny + TJ - 1) / TJ, (g.nx + CIB - 1) / CIB);
+        for (auto f : fb) {
+            les_status st = check_cuda(c, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b),
+                                       "smem attribute");
+            if (st) return st;
+        }
+    const int tiles_a = ((g.nz + A_TK - 1) / A_TK) * ((g.ny + A_TJ - 1) / A_TJ);
+    const int tiles_b = ((g.nz + tk_b - 1) / tk_b) * ((g.ny + tj_b - 1) / tj_b);
+    const int CIA = chunk_len(c, (const void*)k_pass_a<false>, 0, tiles_a, 8);
+    const int CIB = chunk_len(c, fb[1], smem_b, tiles_b, 4 * S > 8 ? 4 * S : 8);
+    const dim3 ga((g.nz + A_TK - 1) / A_TK, (g.ny + A_TJ - 1) / A_TJ, (g.nx + CIA - 1) / CIA);
     auto pass_b = [&](bool first, const float* rin, float* rout, const float* p) -> les_status {
         switch (S) {
-        case 0: return launch_b<0>(c, first, gb, A, CIB, cf, rin, rout, q, p, e, z, in, out, o->max_iter);
-        case 1: return launch_b<1>(c, first, gb, A, CIB, cf, rin, rout, q, p, e, z, in, out, o->max_iter);
-        case 2: return launch_b<2>(c, first, gb, A, CIB, cf, rin, rout, q, p, e, z, in, out, o->max_iter);
-        case 3: return launch_b<3>(c, first, gb, A, CIB, cf, rin, rout, q, p, e, z, in, out, o->max_iter);
-        case 4: return launch_b<4>(c, first, gb, A, CIB, cf, rin, rout, q, p, e, z, in, out, o->max_iter);
-        case 5: return launch_b<5>(c, first, gb, A, CIB, cf, rin, rout, q, p, e, z, in, out, o->max_iter);
-        default: return launch_b<6>(c, first, gb, A, CIB, cf, rin, rout, q, p, e, z, in, out, o->max_iter);
+        case 0: return launch_b<0>(c, first, CIB, A, cf, rin, rout, q, p, e, z, in, out, o->max_iter);
+        case 1: return launch_b<1>(c, first, CIB, A, cf, rin, rout, q, p, e, z, in, out, o->max_iter);
+        case 2: return launch_b<2>(c, first, CIB, A, cf, rin, rout, q, p, e, z, in, out, o->max_iter);
+        case 3: return launch_b<3>(c, first, CIB, A, cf, rin, rout, q, p, e, z, in, out, o->max_iter);
+        case 4: return launch_b<4>(c, first, CIB, A, cf, rin, rout, q, p, e, z, in, out, o->max_iter);
+        case 5: return launch_b<5>(c, first, CIB, A, cf, rin, rout, q, p, e, z, in, out, o->max_iter);
+        default: return launch_b<6>(c, first, CIB, A, cf, rin, rout, q, p, e, z, in, out, o->max_iter);
         }
     };
-    int rc = 0;
     les_status st = pass_b(true, r[0], r[1], pb[0]);   // z = M^-1 r, rho, e = 0
     if (st) return st;
-    rc = 1;
-    int pc = 0, launched = 0, batch = 4;
+    int rc = 1, pc = 0, launched = 0, batch = 4;
     for (;;) {
         for (int it = 0; it < batch; ++it) {
             auto ka = (launched + it == 0) ? k_pass_a<true> : k_pass_a<false>;
-            launch_p(c, PROF_IN_SPMV, ka, ga, dim3(TK, TJ), g, A, CIA, (const float*)z, (const float*)pb[pc],
+            launch_p(c, PROF_IN_SPMV, ka, ga, dim3(NT), g, A, CIA, (const float*)z, (const float*)pb[pc],
                      pb[pc ^ 1], q, c->partials, c->counters + 15, in);
             pc ^= 1;
             st = pass_b(false, r[rc], r[rc ^ 1], pb[pc]);
