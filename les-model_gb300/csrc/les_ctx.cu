@@ -193,6 +193,7 @@ void les_destroy(les_ctx* c)
     if (c->h_state) cudaFreeHost(c->h_state);
     for (auto& e : c->prof_ev) cudaEventDestroy(e);
     for (auto& e : c->marks) cudaEventDestroy(e);
+    les::tma_cache_free(c->tma);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -336,6 +337,7 @@ les_status les_set_option(les_ctx* c, int option, int value)
     if (!c) return LES_BAD_ARG;
     switch (option) {
     case LES_OPT_FUSED: c->fused = value ? 1 : 0; return LES_OK;
+    case LES_OPT_TMA: c->opt_tma = value ? 1 : 0; return LES_OK;
     default: return fail(c, LES_BAD_ARG, "unknown option");
     }
 }

@@ -26,6 +26,7 @@
 
 #include "les_internal.cuh"
 #include "les_mixed.cuh"
+#include "les_tma.cuh"
 
 using namespace les;
 
@@ -61,12 +62,6 @@ __device__ __forceinline__ double acc_value(const Acc& a) { return (double)a.hi 
 
 __device__ __forceinline__ int imin(int a, int b) { return a < b ? a : b; }
 __device__ __forceinline__ int imax(int a, int b) { return a > b ? a : b; }
-
-// 7-point product at a cell whose code is `cd`, with the centre value zc and
-// the six neighbours (read only where the reference's bounds tests allow).
-struct Nb {
-    float w, e, s, n, b, t;
-};
 
 // ---- pass A -----------------------------------------------------------------
 constexpr int A_TK = W - 2;       // 30 output columns
@@ -292,10 +287,342 @@ __global__ void __launch_bounds__(NT) k_pass_b(Geo g, ViewF A, int CI, ChebF cf,
     }
 }
 
+// ---- TMA versions ------------------------------------------------------------
+// The same two passes with every plane of input staged by the Tensor Memory
+// Accelerator: one thread issues cp.async.bulk.tensor copies of the next
+// planes' tiles into a shared-memory ring two planes ahead of the
+// computation, and the block waits on the slot's mbarrier.  Out-of-range halo
+// cells read as zero.  A TMA box must start on a 16-byte boundary in k, so
+// each box starts at the k rounded down to 4 floats (16 bytes for the byte
+// codes) and is a few cells wider; threads index from the remainder.
+// Requires nz % 16 == 0 (16-byte row pitch of the byte-coded stencil).
+
+constexpr int TMA_BX = 36;    // float box width (32 + up to 3 alignment cells, rounded to 16 B)
+constexpr int TMA_CBX = 48;   // code box width (32 + up to 15 alignment cells)
+
+__device__ __forceinline__ int align_down(int x, int a) { return x & ~(a - 1); }
+
+// error path of a timed-out TMA wait: report through the solver state and
+// leave (the host stops on done)
+__device__ __forceinline__ void tma_timeout(SolverState* st)
+{
+    st->status = LES_TIMEOUT;
+    st->done = 1;
+    __threadfence();
+}
+
+constexpr int A2_SLOT = 2 * TMA_BX * A_H * 4 + TMA_CBX * A_H;   // z, pold, code = 5376 B
+constexpr int A2_RING = 4;
+
+template <bool FIRST>
+__global__ void __launch_bounds__(NT) k_pass_a_tma(Geo g, ViewF A, int CI, const __grid_constant__ CUtensorMap mz,
+                                                    const __grid_constant__ CUtensorMap mp,
+                                                    const __grid_constant__ CUtensorMap mc, float* __restrict__ pnew,
+                                                    float* __restrict__ q, double* partials, unsigned* counter,
+                                                    SolverState* st)
+{
+    __shared__ __align__(128) unsigned char ring[A2_RING][A2_SLOT];
+    __shared__ float sp[3][A_PL];
+    __shared__ uint8_t sc[3][A_PL];
+    __shared__ __align__(8) uint64_t bar[A2_RING];
+    __shared__ double sm[32];
+    if (st->done) return;
+    const float beta = FIRST ? 0.f : (float)st->beta;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int k0 = blockIdx.x * A_TK, j0 = blockIdx.y * A_TJ;
+    const int i0 = blockIdx.z * CI, i1 = imin(g.nx, i0 + CI);
+    const int kg = k0 - 1 + lane;
+    const bool kin = kg >= 0 && kg < g.nz;
+    const bool kcen = lane >= 1 && lane <= A_TK && kg < g.nz;
+    const int xf = align_down(k0 - 1, 4), of = (k0 - 1) - xf;
+    const int xc = align_down(k0 - 1, 16), oc = (k0 - 1) - xc;
+    constexpr unsigned FB = TMA_BX * A_H * 4, CB = TMA_CBX * A_H;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < A2_RING; ++s) mbar_init(&bar[s], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    const int Pbeg = imax(i0 - 1, 0), Pend = imin(i1, g.nx - 1);   // planes loaded: [Pbeg, Pend]
+    auto issue = [&](int P) {
+        const int s = P % A2_RING;
+        unsigned char* dst = ring[s];
+        mbar_arrive_expect_tx(&bar[s], FIRST ? FB + CB : 2 * FB + CB);
+        tma_load_3d(dst, &mz, &bar[s], xf, j0 - 1, P);
+        if (!FIRST) tma_load_3d(dst + FB, &mp, &bar[s], xf, j0 - 1, P);
+        tma_load_3d(dst + 2 * FB, &mc, &bar[s], xc, j0 - 1, P);
+    };
+    if (threadIdx.x == 0)
+        for (int P = Pbeg; P <= imin(Pbeg + 1, Pend); ++P) issue(P);
+    unsigned phase = 0;   // bit s: parity of the next wait on slot s
+    Acc acc;
+    for (int P = i0 - 1; P <= i1; ++P) {
+        if (P >= Pbeg && P <= Pend) {
+            if (threadIdx.x == 0 && P + 2 <= Pend) issue(P + 2);
+            const int s = P % A2_RING;
+            if (!mbar_wait_bounded(&bar[s], (phase >> s) & 1u)) {
+                tma_timeout(st);
+                mbar_wait_bounded(&bar[s], (phase >> s) & 1u);   // let a late copy land before leaving
+                return;
+            }
+            phase ^= 1u << s;
+            const float* tz = reinterpret_cast<const float*>(ring[s]);
+            const float* tp = tz + TMA_BX * A_H;
+            const uint8_t* tc = ring[s] + 2 * FB;
+            float* buf = sp[P % 3];
+            uint8_t* cbuf = sc[P % 3];
+#pragma unroll
+            for (int rr = 0; rr < A_H / NW; ++rr) {
+                const int row = warp + rr * NW;
+                const int j = j0 - 1 + row;
+                const int pt = row * W + lane;
+                float v = 0.f;
+                if (kin && j >= 0 && j < g.ny) {
+                    const float zz = tz[row * TMA_BX + of + lane];
+                    v = FIRST ? zz : fmaf(beta, tp[row * TMA_BX + of + lane], zz);
+                    if (kcen && row >= 1 && row <= A_TJ && P >= i0 && P < i1) pnew[P * g.si + j * g.sj + kg] = v;
+                }
+                buf[pt] = v;
+                cbuf[pt] = tc[row * TMA_CBX + oc + lane];
+            }
+        }
+        __syncthreads();
+        const int C = P - 1;
+        if (C >= i0 && C < i1 && kcen) {
+            const float* cb = sp[C % 3];
+            const float* cw = sp[(C + 2) % 3];
+            const float* ce = sp[(C + 1) % 3];
+            const uint8_t* cc = sc[C % 3];
+            for (int row = 1 + warp; row <= A_TJ; row += NW) {
+                const int j = j0 - 1 + row;
+                if (j >= g.ny) break;
+                const int pt = row * W + lane;
+                const float pc = cb[pt];
+                float val;
+                if (cc[pt] == 1u) {
+                    val = A.k.c0 * pc + A.k.x1 * (cw[pt] + ce[pt]) + A.k.y1 * (cb[pt - W] + cb[pt + W]) +
+                          A.k.z1 * (cb[pt - 1] + cb[pt + 1]);
+                } else {
+                    CoefF a = A.at(C * g.si + j * g.sj + kg);
+                    val = a.c * pc;
+                    if (C > 0) val += a.w * cw[pt];
+                    if (C < g.nx - 1) val += a.e * ce[pt];
+                    if (j > 0) val += a.s * cb[pt - W];
+                    if (j < g.ny - 1) val += a.n * cb[pt + W];
+                    if (kg > 0) val += a.b * cb[pt - 1];
+                    if (kg < g.nz - 1) val += a.t * cb[pt + 1];
+                }
+                q[C * g.si + j * g.sj + kg] = val;
+                acc_prod(acc, pc, val);
+            }
+        }
+        __syncthreads();
+    }
+    double v[1] = {acc_value(acc)};
+    if (last_block_sum<1>(v, partials, counter, sm)) {
+        if (threadIdx.x == 0) st->alpha = st->rho / v[0];
+    }
+}
+
+template <int S>
+struct BTma {
+    static constexpr int H = BGeom<S>::H;
+    static constexpr unsigned FB = TMA_BX * H * 4;        // r or q box
+    static constexpr unsigned CB = TMA_CBX * H;           // code box
+    static constexpr unsigned EB = W * BGeom<S>::TJ * 4;  // e or p box (output tile)
+    static constexpr unsigned R128(unsigned b) { return (b + 127u) & ~127u; }
+    static constexpr unsigned OFF_Q = R128(FB), OFF_C = OFF_Q + R128(FB), OFF_E = OFF_C + R128(CB),
+                              OFF_P = OFF_E + R128(EB), SLOT = OFF_P + R128(EB);
+    static constexpr int RING = 3;
+    // ring, then the compute rings of BGeom, then the barriers
+    // + 128: the kernel aligns the dynamic shared-memory base to 128 bytes
+    static constexpr size_t BYTES = (size_t)RING * SLOT + ((BGeom<S>::BYTES + 127) & ~(size_t)127) + 64 + 128;
+};
+
+template <int S, bool FIRST>
+__global__ void __launch_bounds__(NT) k_pass_b_tma(Geo g, ViewF A, int CI, ChebF cf,
+                                                    const __grid_constant__ CUtensorMap mr,
+                                                    const __grid_constant__ CUtensorMap mq,
+                                                    const __grid_constant__ CUtensorMap mc,
+                                                    const __grid_constant__ CUtensorMap me,
+                                                    const __grid_constant__ CUtensorMap mp, float* __restrict__ r_out,
+                                                    float* __restrict__ e, float* __restrict__ z_out,
+                                                    double* partials, unsigned* counter, SolverState* st,
+                                                    SolverState* outer, int total_cap)
+{
+    using GB = BGeom<S>;
+    using TB = BTma<S>;
+    constexpr int TK = GB::TK, TJ = GB::TJ, H = GB::H, PL = GB::PL;
+    extern __shared__ __align__(128) unsigned char dyn_raw[];
+    __shared__ double sm[64];
+    if (st->done) return;
+    // TMA destinations must be 128-byte aligned
+    unsigned char* dyn = dyn_raw + ((128u - (smem_addr(dyn_raw) & 127u)) & 127u);
+    unsigned char* ring = dyn;
+    float* rp = reinterpret_cast<float*>(dyn + TB::RING * TB::SLOT);
+    float* zr = rp + (S + 1) * PL;
+    float* pcr = zr + 3 * S * PL;
+    uint8_t* cr = reinterpret_cast<uint8_t*>(rp + GB::FLOATS);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(dyn + TB::RING * TB::SLOT + ((GB::BYTES + 127) & ~(size_t)127));
+    const float alpha = FIRST ? 0.f : (float)st->alpha;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int k0 = blockIdx.x * TK, j0 = blockIdx.y * TJ;
+    const int i0 = blockIdx.z * CI, i1 = imin(g.nx, i0 + CI);
+    const int kg = k0 - S + lane;
+    const bool kin = kg >= 0 && kg < g.nz;
+    const bool kcen = lane >= S && lane < S + TK && kin;
+    const int xf = align_down(k0 - S, 4), of = (k0 - S) - xf;
+    const int xc = align_down(k0 - S, 16), oc = (k0 - S) - xc;
+    const int xe = align_down(k0, 4), oe = k0 - xe;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TB::RING; ++s) mbar_init(&bar[s], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    const int Ibeg = imax(i0 - S, 0), Iend = imin(i1 + S, g.nx) - 1;   // planes loaded
+    auto issue = [&](int I) {
+        const int s = I % TB::RING;
+        unsigned char* dst = ring + s * TB::SLOT;
+        const bool centre = I >= i0 && I < i1 && !FIRST;
+        mbar_arrive_expect_tx(&bar[s], (FIRST ? TB::FB : 2 * TB::FB) + TB::CB + (centre ? 2 * TB::EB : 0));
+        tma_load_3d(dst, &mr, &bar[s], xf, j0 - S, I);
+        if (!FIRST) tma_load_3d(dst + TB::OFF_Q, &mq, &bar[s], xf, j0 - S, I);
+        tma_load_3d(dst + TB::OFF_C, &mc, &bar[s], xc, j0 - S, I);
+        if (centre) {
+            tma_load_3d(dst + TB::OFF_E, &me, &bar[s], xe, j0, I);
+            tma_load_3d(dst + TB::OFF_P, &mp, &bar[s], xe, j0, I);
+        }
+    };
+    if (threadIdx.x == 0)
+        for (int I = Ibeg; I <= imin(Ibeg + 1, Iend); ++I) issue(I);
+    unsigned phase = 0;
+    Acc arr, arz;
+    for (int I = i0 - S; I < i1 + S; ++I) {
+        if (I >= Ibeg && I <= Iend) {
+            if (threadIdx.x == 0 && I + 2 <= Iend) issue(I + 2);
+            const int s = I % TB::RING;
+            if (!mbar_wait_bounded(&bar[s], (phase >> s) & 1u)) {
+                tma_timeout(st);
+                mbar_wait_bounded(&bar[s], (phase >> s) & 1u);   // let a late copy land before leaving
+                return;
+            }
+            phase ^= 1u << s;
+            const unsigned char* sl = ring + s * TB::SLOT;
+            const float* tr = reinterpret_cast<const float*>(sl);
+            const float* tq = reinterpret_cast<const float*>(sl + TB::OFF_Q);
+            const uint8_t* tc = sl + TB::OFF_C;
+            const float* te = reinterpret_cast<const float*>(sl + TB::OFF_E);
+            const float* tp = reinterpret_cast<const float*>(sl + TB::OFF_P);
+            const int slot = I % (S + 1);
+            float* rpl = rp + slot * PL;
+            uint8_t* crl = cr + slot * PL;
+            float* z0 = zr + (I % 3) * PL;
+            const bool plane_out = I >= i0 && I < i1;
+            for (int row = warp; row < H; row += NW) {
+                const int j = j0 - S + row;
+                if (!kin || j < 0 || j >= g.ny) continue;
+                const int pt = row * W + lane;
+                const float rold = tr[row * TMA_BX + of + lane];
+                const float rv = FIRST ? rold : fmaf(-alpha, tq[row * TMA_BX + of + lane], rold);
+                rpl[pt] = rv;
+                const uint8_t cd = tc[row * TMA_CBX + oc + lane];
+                crl[pt] = cd;
+                if (S > 0) z0[pt] = cf.a0 * rv;
+                if (plane_out && kcen && row >= S && row < S + TJ) {
+                    const int id = I * g.si + j * g.sj + kg;
+                    const int ept = (row - S) * W + oe + (lane - S);
+                    r_out[id] = rv;
+                    e[id] = FIRST ? 0.f : fmaf(alpha, tp[ept], te[ept]);
+                    acc_prod(arr, rv, rv);
+                    if (S == 0) {
+                        const float zv = rv * (cd == 0 ? 1.f : 1.f / A.k.c0);
+                        z_out[id] = zv;
+                        acc_prod(arz, rv, zv);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int lv = 1; lv <= S; ++lv) {
+            const int Pk = I - lv;
+            if (Pk >= imax(0, i0 - S + lv) && Pk < imin(g.nx, i1 + S - lv) && kin && lane >= lv &&
+                lane < W - lv) {
+                const float* zc = zr + ((lv - 1) * 3 + Pk % 3) * PL;
+                const float* zw = zr + ((lv - 1) * 3 + (Pk + 2) % 3) * PL;
+                const float* ze = zr + ((lv - 1) * 3 + (Pk + 1) % 3) * PL;
+                const float* rpl = rp + (Pk % (S + 1)) * PL;
+                const uint8_t* crl = cr + (Pk % (S + 1)) * PL;
+                const float* pcp = lv >= 2 ? pcr + ((lv - 2) * 2 + Pk % 2) * PL : rpl;
+                float* zo = lv < S ? zr + (lv * 3 + Pk % 3) * PL : nullptr;
+                float* po = lv < S ? pcr + ((lv - 1) * 2 + Pk % 2) * PL : nullptr;
+                const bool out_lane = lv == S && kcen && Pk >= i0 && Pk < i1;
+                for (int row = lv + warp; row < H - lv; row += NW) {
+                    const int j = j0 - S + row;
+                    if (j < 0 || j >= g.ny) continue;
+                    const int pt = row * W + lane;
+                    const unsigned cd = crl[pt];
+                    const float zcv = zc[pt];
+                    float az;
+                    if (cd == 1u) {
+                        az = A.k.c0 * zcv + A.k.x1 * (zw[pt] + ze[pt]) + A.k.y1 * (zc[pt - W] + zc[pt + W]) +
+                             A.k.z1 * (zc[pt - 1] + zc[pt + 1]);
+                    } else {
+                        CoefF a = A.at(Pk * g.si + j * g.sj + kg);
+                        az = a.c * zcv;
+                        if (Pk > 0) az += a.w * zw[pt];
+                        if (Pk < g.nx - 1) az += a.e * ze[pt];
+                        if (j > 0) az += a.s * zc[pt - W];
+                        if (j < g.ny - 1) az += a.n * zc[pt + W];
+                        if (kg > 0) az += a.b * zc[pt - 1];
+                        if (kg < g.nz - 1) az += a.t * zc[pt + 1];
+                    }
+                    const float rv = rpl[pt];
+                    const float pck = fmaf(cf.b[lv - 1], pcp[pt], rv - az);
+                    const float zk = fmaf(cf.a[lv - 1], pck, zcv);
+                    if (lv < S) {
+                        zo[pt] = zk;
+                        po[pt] = pck;
+                    } else if (out_lane && row >= S && row < S + TJ) {
+                        z_out[Pk * g.si + j * g.sj + kg] = zk;
+                        acc_prod(arz, rv, zk);
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    double v[2] = {acc_value(arr), acc_value(arz)};
+    if (last_block_sum<2>(v, partials, counter, sm)) {
+        if (threadIdx.x == 0) {
+            if (FIRST) {
+                st->rho = v[1];
+            } else {
+                const double err = sqrt(v[0]);
+                const int kk = st->k + 1;
+                st->k = kk;
+                st->err = err;
+                const int total = outer->iters + 1;
+                outer->iters = total;
+                if (err < st->tol) { st->done = 1; st->status = LES_OK; }
+                else if (!isfinite(err)) { st->done = 1; st->status = LES_NONFINITE; }
+                else if (kk >= st->max_iter || total >= total_cap) { st->done = 1; st->status = LES_NOT_CONVERGED; }
+                st->beta = v[1] / st->rho;
+                st->rho = v[1];
+            }
+        }
+    }
+}
+
 template <int S>
 const void* pass_b_fn(bool first)
 {
     return first ? (const void*)k_pass_b<S, true> : (const void*)k_pass_b<S, false>;
+}
+
+template <int S>
+const void* pass_b_tma_fn(bool first)
+{
+    return first ? (const void*)k_pass_b_tma<S, true> : (const void*)k_pass_b_tma<S, false>;
 }
 
 template <int S>
@@ -332,6 +659,69 @@ int chunk_len(les_ctx* c, const void* fn, size_t smem, int tiles, int min_ci)
 
 namespace les {
 
+bool tma_encode_3d(CUtensorMap* map, CUtensorMapDataType dtype, size_t esize, void* base, int nx, int ny, int nz,
+                   unsigned bx, unsigned by)
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+        else
+            cudaGetLastError();
+    }
+    if (!encode) return false;
+    cuuint64_t dims[3] = {(cuuint64_t)nz, (cuuint64_t)ny, (cuuint64_t)nx};
+    cuuint64_t strides[2] = {(cuuint64_t)nz * esize, (cuuint64_t)ny * nz * esize};
+    cuuint32_t box[3] = {bx, by, 1};
+    cuuint32_t es[3] = {1, 1, 1};
+    return encode(map, dtype, 3, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Tensor maps over the inner-solve vectors, built once per context and
+// Chebyshev degree (the boxes of pass B depend on the halo).
+struct TmaCache {
+    int S = -1;
+    bool ok = false;
+    CUtensorMap a_z, a_p[2], a_c;                 // pass A: z, p_old (ping-pong), codes
+    CUtensorMap b_r[2], b_q, b_c, b_e, b_p[2];    // pass B
+};
+
+void tma_cache_free(TmaCache* t) { delete t; }
+
+static bool build_tma(les_ctx* c, int S)
+{
+    if (!c->tma) c->tma = new TmaCache();
+    TmaCache& t = *c->tma;
+    if (t.S == S) return t.ok;
+    const Geo& g = c->g;
+    const unsigned H = 16 + 2 * S;
+    const auto F = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    const auto U8 = CU_TENSOR_MAP_DATA_TYPE_UINT8;
+    bool ok = g.nz % 16 == 0 && c->code != nullptr;
+    ok = ok && tma_encode_3d(&t.a_z, F, 4, c->f[1], g.nx, g.ny, g.nz, TMA_BX, A_H);
+    ok = ok && tma_encode_3d(&t.a_p[0], F, 4, c->f[2], g.nx, g.ny, g.nz, TMA_BX, A_H);
+    ok = ok && tma_encode_3d(&t.a_p[1], F, 4, c->f[3], g.nx, g.ny, g.nz, TMA_BX, A_H);
+    ok = ok && tma_encode_3d(&t.a_c, U8, 1, c->code, g.nx, g.ny, g.nz, TMA_CBX, A_H);
+    ok = ok && tma_encode_3d(&t.b_r[0], F, 4, c->f[0], g.nx, g.ny, g.nz, TMA_BX, H);
+    ok = ok && tma_encode_3d(&t.b_r[1], F, 4, c->f[6], g.nx, g.ny, g.nz, TMA_BX, H);
+    ok = ok && tma_encode_3d(&t.b_q, F, 4, c->f[4], g.nx, g.ny, g.nz, TMA_BX, H);
+    ok = ok && tma_encode_3d(&t.b_c, U8, 1, c->code, g.nx, g.ny, g.nz, TMA_CBX, H);
+    ok = ok && tma_encode_3d(&t.b_e, F, 4, c->f[5], g.nx, g.ny, g.nz, W, 16);
+    ok = ok && tma_encode_3d(&t.b_p[0], F, 4, c->f[2], g.nx, g.ny, g.nz, W, 16);
+    ok = ok && tma_encode_3d(&t.b_p[1], F, 4, c->f[3], g.nx, g.ny, g.nz, W, 16);
+    t.S = S;
+    t.ok = ok;
+    return ok;
+}
+
 bool fused_supported(const les_pcg_opts* o)
 {
     if (o->precond == LES_PC_JACOBI) return true;
@@ -360,14 +750,19 @@ les_status inner_solve_fused(les_ctx* c, const les_pcg_opts* o, ViewF A, SolverS
     }
     float* r[2] = {c->f[0], c->f[6]};
     float *z = c->f[1], *pb[2] = {c->f[2], c->f[3]}, *q = c->f[4], *e = c->f[5];
+    const bool tma = c->opt_tma && build_tma(c, S);
 
     size_t smem_b = 0;
     int tk_b = W, tj_b = 16;
     const void* fb[2] = {};
     switch (S) {
-#define LES_CASE(s)                                                          \
-    case s: smem_b = BGeom<s>::BYTES; tk_b = BGeom<s>::TK; tj_b = BGeom<s>::TJ; \
-        fb[0] = pass_b_fn<s>(true); fb[1] = pass_b_fn<s>(false); break;
+#define LES_CASE(s)                                                                              \
+    case s:                                                                                      \
+        smem_b = tma ? BTma<s>::BYTES : BGeom<s>::BYTES;                                        \
+        tk_b = BGeom<s>::TK; tj_b = BGeom<s>::TJ;                                               \
+        fb[0] = tma ? pass_b_tma_fn<s>(true) : pass_b_fn<s>(true);                               \
+        fb[1] = tma ? pass_b_tma_fn<s>(false) : pass_b_fn<s>(false);                             \
+        break;
         LES_CASE(0) LES_CASE(1) LES_CASE(2) LES_CASE(3) LES_CASE(4) LES_CASE(5)
     default: LES_CASE(6)
 #undef LES_CASE
@@ -380,30 +775,60 @@ les_status inner_solve_fused(les_ctx* c, const les_pcg_opts* o, ViewF A, SolverS
         }
     const int tiles_a = ((g.nz + A_TK - 1) / A_TK) * ((g.ny + A_TJ - 1) / A_TJ);
     const int tiles_b = ((g.nz + tk_b - 1) / tk_b) * ((g.ny + tj_b - 1) / tj_b);
-    const int CIA = chunk_len(c, (const void*)k_pass_a<false>, 0, tiles_a, 8);
+    const void* fa = tma ? (const void*)k_pass_a_tma<false> : (const void*)k_pass_a<false>;
+    const int CIA = chunk_len(c, fa, 0, tiles_a, 8);
     const int CIB = chunk_len(c, fb[1], smem_b, tiles_b, 4 * S > 8 ? 4 * S : 8);
     const dim3 ga((g.nz + A_TK - 1) / A_TK, (g.ny + A_TJ - 1) / A_TJ, (g.nx + CIA - 1) / CIA);
-    auto pass_b = [&](bool first, const float* rin, float* rout, const float* p) -> les_status {
-        switch (S) {
-        case 0: return launch_b<0>(c, first, CIB, A, cf, rin, rout, q, p, e, z, in, out, o->max_iter);
-        case 1: return launch_b<1>(c, first, CIB, A, cf, rin, rout, q, p, e, z, in, out, o->max_iter);
-        case 2: return launch_b<2>(c, first, CIB, A, cf, rin, rout, q, p, e, z, in, out, o->max_iter);
-        case 3: return launch_b<3>(c, first, CIB, A, cf, rin, rout, q, p, e, z, in, out, o->max_iter);
-        case 4: return launch_b<4>(c, first, CIB, A, cf, rin, rout, q, p, e, z, in, out, o->max_iter);
-        case 5: return launch_b<5>(c, first, CIB, A, cf, rin, rout, q, p, e, z, in, out, o->max_iter);
-        default: return launch_b<6>(c, first, CIB, A, cf, rin, rout, q, p, e, z, in, out, o->max_iter);
+    const dim3 gb((g.nz + tk_b - 1) / tk_b, (g.ny + tj_b - 1) / tj_b, (g.nx + CIB - 1) / CIB);
+
+    auto pass_b = [&](bool first, int rin, int pcur) -> les_status {
+        if (!tma) {
+            switch (S) {
+            case 0: return launch_b<0>(c, first, CIB, A, cf, r[rin], r[rin ^ 1], q, pb[pcur], e, z, in, out, o->max_iter);
+            case 1: return launch_b<1>(c, first, CIB, A, cf, r[rin], r[rin ^ 1], q, pb[pcur], e, z, in, out, o->max_iter);
+            case 2: return launch_b<2>(c, first, CIB, A, cf, r[rin], r[rin ^ 1], q, pb[pcur], e, z, in, out, o->max_iter);
+            case 3: return launch_b<3>(c, first, CIB, A, cf, r[rin], r[rin ^ 1], q, pb[pcur], e, z, in, out, o->max_iter);
+            case 4: return launch_b<4>(c, first, CIB, A, cf, r[rin], r[rin ^ 1], q, pb[pcur], e, z, in, out, o->max_iter);
+            case 5: return launch_b<5>(c, first, CIB, A, cf, r[rin], r[rin ^ 1], q, pb[pcur], e, z, in, out, o->max_iter);
+            default: return launch_b<6>(c, first, CIB, A, cf, r[rin], r[rin ^ 1], q, pb[pcur], e, z, in, out, o->max_iter);
+            }
         }
+        const TmaCache& t = *c->tma;
+        cudaEvent_t e1 = nullptr;
+        if (c->prof_on) prof_begin(c, PROF_IN_CHEB, &e1);
+        const void* fn = fb[first ? 0 : 1];
+        float* rout = r[rin ^ 1];
+        double* parts = c->partials;
+        unsigned* cnt = c->counters + 14;
+        int CI = CIB, cap = o->max_iter;
+        Geo gg = g;
+        ViewF AA = A;
+        ChebF cff = cf;
+        void* args[] = {&gg, &AA, &CI, &cff, (void*)&t.b_r[rin], (void*)&t.b_q, (void*)&t.b_c, (void*)&t.b_e,
+                        (void*)&t.b_p[pcur], &rout, &e, &z, &parts, &cnt, &in, &out, &cap};
+        les_status st = check_cuda(c, cudaLaunchKernel(fn, gb, dim3(NT), args, smem_b, c->stream), "pass B (TMA)");
+        ++c->launches;
+        if (e1) cudaEventRecord(e1, c->stream);
+        return st;
     };
-    les_status st = pass_b(true, r[0], r[1], pb[0]);   // z = M^-1 r, rho, e = 0
+    les_status st = pass_b(true, 0, 0);   // z = M^-1 r, rho, e = 0
     if (st) return st;
     int rc = 1, pc = 0, launched = 0, batch = 4;
     for (;;) {
         for (int it = 0; it < batch; ++it) {
-            auto ka = (launched + it == 0) ? k_pass_a<true> : k_pass_a<false>;
-            launch_p(c, PROF_IN_SPMV, ka, ga, dim3(NT), g, A, CIA, (const float*)z, (const float*)pb[pc],
-                     pb[pc ^ 1], q, c->partials, c->counters + 15, in);
+            const bool first = launched + it == 0;
+            if (tma) {
+                const TmaCache& t = *c->tma;
+                auto ka = first ? k_pass_a_tma<true> : k_pass_a_tma<false>;
+                launch_p(c, PROF_IN_SPMV, ka, ga, dim3(NT), g, A, CIA, t.a_z, t.a_p[pc], t.a_c, pb[pc ^ 1], q,
+                         c->partials, c->counters + 15, in);
+            } else {
+                auto ka = first ? k_pass_a<true> : k_pass_a<false>;
+                launch_p(c, PROF_IN_SPMV, ka, ga, dim3(NT), g, A, CIA, (const float*)z, (const float*)pb[pc],
+                         pb[pc ^ 1], q, c->partials, c->counters + 15, in);
+            }
             pc ^= 1;
-            st = pass_b(false, r[rc], r[rc ^ 1], pb[pc]);
+            st = pass_b(false, rc, pc);
             if (st) return st;
             rc ^= 1;
         }
@@ -415,6 +840,7 @@ les_status inner_solve_fused(les_ctx* c, const les_pcg_opts* o, ViewF A, SolverS
         if (c->h_state[1].done || launched >= inner_cap) break;
         batch = batch < 32 ? batch * 2 : 32;
     }
+    if (c->h_state[1].status == LES_TIMEOUT) return fail(c, LES_TIMEOUT, "a TMA wait in the inner solve timed out");
     return LES_OK;
 }
 

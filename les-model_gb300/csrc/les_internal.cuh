@@ -19,6 +19,9 @@
 
 namespace les {
 
+struct TmaCache;                       // tensor maps of the fused passes (les_fused.cu)
+void tma_cache_free(TmaCache* t);
+
 // ---- geometry -------------------------------------------------------------
 struct Geo {
     int nx, ny, nz;
@@ -263,6 +266,8 @@ struct les_ctx {
     double* A[7] = {};
     bool A_valid = false;         // A[] holds the current matrix (stored, or expanded codes)
     int fused = 1;                // LES_OPT_FUSED: fused FP32 inner passes
+    int opt_tma = 1;              // LES_OPT_TMA: TMA-staged fused passes where the grid allows
+    struct les::TmaCache* tma = nullptr;
     les::StencilCoef coef{};
     double* L[7] = {};
     bool have_L = false;

@@ -217,3 +217,32 @@ def test_fused_inner_matches_unfused(shape, pc, deg):
     assert r1 < tol and r0 < tol
     assert abs(i1 - i0) <= max(2, 0.15 * i0), (i1, i0)
     assert maxrel(x1, x0) < 1e-6, maxrel(x1, x0)
+
+
+@pytest.mark.parametrize("shape", [(61, 37, 64), (40, 21, 32)], ids=["61x37x64", "40x21x32"])
+@pytest.mark.parametrize("pc,deg", [(G.PC_CHEBYSHEV, 4), (G.PC_CHEBYSHEV, 6), (G.PC_JACOBI, 0)],
+                         ids=["cheb4", "cheb6", "jacobi"])
+def test_tma_fused_matches_plain_fused(shape, pc, deg):
+    """With nz % 16 == 0 the fused passes stage their planes with TMA; the
+    result must match the same passes with plain loads (identical arithmetic:
+    equal iteration counts, pressure equal to rounding of the final outer
+    correction) and the unfused path (mixed-vs-FP64 bar)."""
+    m, b, lmax = _odd_system(shape, sum(shape) + deg)
+    tol = 1e-8 * np.linalg.norm(b)
+    res = {}
+    for tma, fused in ((1, 1), (0, 1), (0, 0)):
+        with G.Context(m) as c:
+            c.set_option(G.OPT_FUSED, fused)
+            c.set_option(G.OPT_TMA, tma)
+            c.upload_mask(np.zeros(m.n, np.uint8))
+            c.build_stencil()
+            c.upload("b", b)
+            c.upload("p", np.zeros(m.n))
+            st, r = c.pcg(G.pcg_opts(precond=pc, max_iter=20000, tol=tol, lambda_min=3 * np.pi ** 2,
+                                     lambda_max=lmax, degree=max(deg, 1), precision=G.MIXED, inner_rtol=1e-4))
+            res[(tma, fused)] = (st, r.iters, r.outer, r.residual, c.download("p"))
+    t, f, u = res[(1, 1)], res[(0, 1)], res[(0, 0)]
+    assert t[0] == G.OK and f[0] == G.OK and u[0] == G.OK, (t[:4], f[:4], u[:4])
+    assert t[1] == f[1] and t[2] == f[2], (t[:4], f[:4])
+    assert maxrel(t[4], f[4]) < 1e-12, maxrel(t[4], f[4])
+    assert maxrel(t[4], u[4]) < 1e-6, maxrel(t[4], u[4])
