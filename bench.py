@@ -46,7 +46,7 @@ FALLBACK_HBM_GBS = 6800.0
 # measured by the FP64 GPU path (whose counts match the reference's within
 # +-1 in the parity tests); used by the reference arm to extrapolate its
 # bounded per-step sample to a full solve.
-REF_ITERS = {"large": 300, "small": 150, "xlarge": 500}
+REF_ITERS = {"large": 545, "small": 240, "xlarge": 1200}
 
 
 def parse():
@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--cpu-iters", type=int, default=12, help="PCG iterations in the CPU sample")
     ap.add_argument("--seed", type=int, default=1234)
+    ap.add_argument("--inner-rtol", type=float, default=1e-4, help="mixed path: inner FP32 solve reduction")
+    ap.add_argument("--tma", type=int, default=0, help="stage the fused passes with TMA (LES_OPT_TMA)")
     return ap.parse_args()
 
 
@@ -149,11 +151,11 @@ def make_ctx(G, les_cases, shape, h, solid, f, dev, precond):
     return c, lmax
 
 
-def step_params(G, les_cases, precond, lmax, precision):
+def step_params(G, les_cases, precond, lmax, precision, inner_rtol=1e-4):
     pc = pc_code(G, precond)
     if precision == G.MIXED:
         opts = G.pcg_opts(precond=pc, max_iter=50000, lambda_min=3 * np.pi ** 2, lambda_max=lmax, degree=4,
-                          precision=G.MIXED, inner_rtol=1e-4, inner_max_iter=5000, max_outer=40)
+                          precision=G.MIXED, inner_rtol=inner_rtol, inner_max_iter=5000, max_outer=40)
     else:
         opts = G.pcg_opts(precond=pc, max_iter=10000, lambda_min=3 * np.pi ** 2, lambda_max=lmax, degree=4)
     return G.step_params(nu=les_cases.NU, rho=les_cases.RHO, cs=les_cases.CS, cfl_conv=les_cases.CFL_CONV,
@@ -257,7 +259,8 @@ def run_ours(args):
     shape, h, solid, f = les_cases.case(args.workload, args.seed)
     n = int(np.prod(shape))
     ctx, lmax = make_ctx(G, les_cases, shape, h, solid, f, dev, args.precond)
-    prm = step_params(G, les_cases, args.precond, lmax, G.MIXED)
+    ctx.set_option(G.OPT_TMA, args.tma)
+    prm = step_params(G, les_cases, args.precond, lmax, G.MIXED, args.inner_rtol)
     ctx64 = None
     if not args.no_fp64:
         ctx64, _ = make_ctx(G, les_cases, shape, h, solid, f, dev, args.precond)
@@ -367,7 +370,8 @@ def run_ours(args):
             "config": {"workload": "%s %s obstacle, %s(4)-PCG mixed FP32/FP64 to rel residual 1e-8" %
                                    (args.workload, "x".join(map(str, shape)), args.precond),
                        "cells": n, "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "flushed (256 MiB write) before every timed step"},
+                       "l2": "flushed (256 MiB write) before every timed step",
+                       "inner_rtol": args.inner_rtol, "tma": args.tma},
             "e2e": e2e, "gpu_launches": launches, "wall_s": wall,
             "iters_inner_mean": statistics.mean(rec["iters"]), "outer_mean": statistics.mean(rec["outer"]),
             "rel_residual_max": max(rec["rres"]), "roofline": roof, "clocks": clk}

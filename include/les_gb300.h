@@ -224,8 +224,9 @@ typedef enum les_option {
     LES_OPT_FUSED = 0,  /* 1 (default): mixed-precision inner iteration as two fused
                            passes (Jacobi, Chebyshev degree 2..7); 0: one kernel per
                            vector operation */
-    LES_OPT_TMA = 1     /* 1 (default): stage the fused passes' planes with TMA when
-                           nz % 16 == 0 and the matrix is device-built; 0: plain loads */
+    LES_OPT_TMA = 1     /* 1: stage the fused passes' planes with TMA when nz % 16 == 0
+                           and the matrix is device-built; 0 (default): plain loads with
+                           register prefetch (higher occupancy, faster on GB300) */
 } les_option;
 les_status les_set_option(les_ctx* ctx, int option, int value);
 

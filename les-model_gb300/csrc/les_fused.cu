@@ -23,6 +23,7 @@
 // and blocks in FP64; GB300's FP64 pipe is ~70x slower than its FP32 pipe, so
 // a per-cell FP64 add tree would dominate these memory-bound kernels.
 #include <cmath>
+#include <type_traits>
 
 #include "les_internal.cuh"
 #include "les_mixed.cuh"
@@ -63,6 +64,24 @@ __device__ __forceinline__ double acc_value(const Acc& a) { return (double)a.hi 
 __device__ __forceinline__ int imin(int a, int b) { return a < b ? a : b; }
 __device__ __forceinline__ int imax(int a, int b) { return a > b ? a : b; }
 
+// The 7-point product at a cell next to a wall, the outlet or a solid (any
+// stencil code but 1): decoded coefficients and the reference's bounds tests
+// (src/pressure.cpp:735-742), on shared-memory planes whose rows are W wide.
+// Rare, so kept out of line.
+__device__ __noinline__ float az_general(const ViewF A, int id, int Pk, int j, int kg, const Geo g, const float* zc,
+                                         const float* zw, const float* ze, int pt)
+{
+    CoefF a = A.at(id);
+    float az = a.c * zc[pt];
+    if (Pk > 0) az += a.w * zw[pt];
+    if (Pk < g.nx - 1) az += a.e * ze[pt];
+    if (j > 0) az += a.s * zc[pt - W];
+    if (j < g.ny - 1) az += a.n * zc[pt + W];
+    if (kg > 0) az += a.b * zc[pt - 1];
+    if (kg < g.nz - 1) az += a.t * zc[pt + 1];
+    return az;
+}
+
 // ---- pass A -----------------------------------------------------------------
 constexpr int A_TK = W - 2;       // 30 output columns
 constexpr int A_TJ = 14;          // output rows
@@ -70,7 +89,7 @@ constexpr int A_H = A_TJ + 2;     // 16 rows with halo = 2 per warp
 constexpr int A_PL = W * A_H;
 
 template <bool FIRST>
-__global__ void __launch_bounds__(NT) k_pass_a(Geo g, ViewF A, int CI, const float* __restrict__ z,
+__global__ void __launch_bounds__(NT, 6) k_pass_a(Geo g, ViewF A, int CI, const float* __restrict__ z,
                                                 const float* __restrict__ pold, float* __restrict__ pnew,
                                                 float* __restrict__ q, double* partials, unsigned* counter,
                                                 SolverState* st)
@@ -85,32 +104,51 @@ __global__ void __launch_bounds__(NT) k_pass_a(Geo g, ViewF A, int CI, const flo
     const int kg = k0 - 1 + lane;
     const bool kin = kg >= 0 && kg < g.nz;
     const bool kcen = lane >= 1 && lane <= A_TK && kg < g.nz;
+    constexpr int RA = A_H / NW;   // rows per warp (2)
+    float nz_[RA], np_[RA];
+    const int Pbeg = imax(i0 - 1, 0), Pend = imin(i1, g.nx - 1);
+    // the next plane's z and p_old are fetched into registers while the
+    // current plane's products run
+    auto fetch = [&](int P) {
+#pragma unroll
+        for (int m = 0; m < RA; ++m) {
+            const int j = j0 - 1 + warp + m * NW;
+            if (kin && j >= 0 && j < g.ny) {
+                const int id = P * g.si + j * g.sj + kg;
+                nz_[m] = z[id];
+                if (!FIRST) np_[m] = pold[id];
+            }
+        }
+    };
+    if (Pbeg <= Pend) fetch(Pbeg);
     Acc acc;
     for (int P = i0 - 1; P <= i1; ++P) {
-        if (P >= 0 && P < g.nx) {
+        if (P >= Pbeg && P <= Pend) {
             float* buf = sp[P % 3];
 #pragma unroll
-            for (int rr = 0; rr < A_H / NW; ++rr) {
-                const int row = warp + rr * NW;
+            for (int m = 0; m < RA; ++m) {
+                const int row = warp + m * NW;
                 const int j = j0 - 1 + row;
                 float v = 0.f;
                 if (kin && j >= 0 && j < g.ny) {
-                    const int id = P * g.si + j * g.sj + kg;
-                    v = FIRST ? z[id] : fmaf(beta, pold[id], z[id]);
-                    if (kcen && row >= 1 && row <= A_TJ && P >= i0 && P < i1) pnew[id] = v;
+                    v = FIRST ? nz_[m] : fmaf(beta, np_[m], nz_[m]);
+                    if (kcen && row >= 1 && row <= A_TJ && P >= i0 && P < i1) pnew[P * g.si + j * g.sj + kg] = v;
                 }
                 buf[row * W + lane] = v;
             }
+            if (P + 1 <= Pend) fetch(P + 1);
         }
         __syncthreads();
         const int C = P - 1;
         if (C >= i0 && C < i1 && kcen) {
-            const float* cb = sp[C % 3];
-            const float* cw = sp[(C + 2) % 3];
-            const float* ce = sp[(C + 1) % 3];
-            for (int row = 1 + warp; row <= A_TJ; row += NW) {
+            const float* __restrict__ cb = sp[C % 3];
+            const float* __restrict__ cw = sp[(C + 2) % 3];
+            const float* __restrict__ ce = sp[(C + 1) % 3];
+#pragma unroll
+            for (int m = 0; m < RA; ++m) {
+                const int row = 1 + warp + m * NW;
                 const int j = j0 - 1 + row;
-                if (j >= g.ny) break;
+                if (row > A_TJ || j >= g.ny) break;
                 const int pt = row * W + lane;
                 const int id = C * g.si + j * g.sj + kg;
                 const float pc = cb[pt];
@@ -119,14 +157,7 @@ __global__ void __launch_bounds__(NT) k_pass_a(Geo g, ViewF A, int CI, const flo
                     val = A.k.c0 * pc + A.k.x1 * (cw[pt] + ce[pt]) + A.k.y1 * (cb[pt - W] + cb[pt + W]) +
                           A.k.z1 * (cb[pt - 1] + cb[pt + 1]);
                 } else {
-                    CoefF a = A.at(id);
-                    val = a.c * pc;
-                    if (C > 0) val += a.w * cw[pt];
-                    if (C < g.nx - 1) val += a.e * ce[pt];
-                    if (j > 0) val += a.s * cb[pt - W];
-                    if (j < g.ny - 1) val += a.n * cb[pt + W];
-                    if (kg > 0) val += a.b * cb[pt - 1];
-                    if (kg < g.nz - 1) val += a.t * cb[pt + 1];
+                    val = az_general(A, id, C, j, kg, g, cb, cw, ce, pt);
                 }
                 q[id] = val;
                 acc_prod(acc, pc, val);
@@ -160,7 +191,7 @@ struct BGeom {
 
 // S = 0: Jacobi (z = r'/A_c, no stencil levels).
 template <int S, bool FIRST>
-__global__ void __launch_bounds__(NT) k_pass_b(Geo g, ViewF A, int CI, ChebF cf, const float* __restrict__ r_in,
+__global__ void __launch_bounds__(NT, 3) k_pass_b(Geo g, ViewF A, int CI, ChebF cf, const float* __restrict__ r_in,
                                                 float* __restrict__ r_out, const float* __restrict__ q,
                                                 const float* __restrict__ p, float* __restrict__ e,
                                                 float* __restrict__ z_out, double* partials, unsigned* counter,
@@ -182,78 +213,102 @@ __global__ void __launch_bounds__(NT) k_pass_b(Geo g, ViewF A, int CI, ChebF cf,
     const int kg = k0 - S + lane;                          // this lane's global k
     const bool kin = kg >= 0 && kg < g.nz;
     const bool kcen = lane >= S && lane < S + TK && kin;
+    // level-0 rows of this warp: warp, warp+8, ... (< H); the next plane's
+    // inputs are fetched into registers while the current plane's Chebyshev
+    // levels run
+    constexpr int R0 = (H + NW - 1) / NW;
+    float nr[R0], nq[R0], ne[R0], np[R0];
+    uint8_t nc[R0];
+    const int Ibeg = imax(i0 - S, 0), Iend = imin(i1 + S, g.nx) - 1;
+    auto fetch = [&](int I) {
+        const bool centre_plane = I >= i0 && I < i1;
+#pragma unroll
+        for (int m = 0; m < R0; ++m) {
+            const int row = warp + m * NW;
+            const int j = j0 - S + row;
+            if (row < H && kin && j >= 0 && j < g.ny) {
+                const int id = I * g.si + j * g.sj + kg;
+                nr[m] = r_in[id];
+                if (!FIRST) nq[m] = q[id];
+                nc[m] = A.code ? A.code[id] : (uint8_t)2;
+                if (!FIRST && centre_plane && kcen && row >= S && row < S + TJ) {
+                    ne[m] = e[id];
+                    np[m] = p[id];
+                }
+            }
+        }
+    };
+    if (Ibeg <= Iend) fetch(Ibeg);
     Acc arr, arz;
     for (int I = i0 - S; I < i1 + S; ++I) {
         // ---- level 0 at plane I: r' = r - alpha q over the tile + S halo
-        if (I >= 0 && I < g.nx) {
+        if (I >= Ibeg && I <= Iend) {
             const int slot = I % (S + 1);
             float* rpl = rp + slot * PL;
             uint8_t* crl = cr + slot * PL;
             float* z0 = zr + (I % 3) * PL;
             const bool plane_out = I >= i0 && I < i1;
-            for (int row = warp; row < H; row += NW) {
+#pragma unroll
+            for (int m = 0; m < R0; ++m) {
+                const int row = warp + m * NW;
                 const int j = j0 - S + row;
                 const int pt = row * W + lane;
-                if (!kin || j < 0 || j >= g.ny) continue;
-                const int id = I * g.si + j * g.sj + kg;
-                const float rold = r_in[id];
-                const float rv = FIRST ? rold : fmaf(-alpha, q[id], rold);
+                if (row >= H || !kin || j < 0 || j >= g.ny) continue;
+                const float rv = FIRST ? nr[m] : fmaf(-alpha, nq[m], nr[m]);
                 rpl[pt] = rv;
-                crl[pt] = A.code ? A.code[id] : (uint8_t)2;
+                crl[pt] = nc[m];
                 if (S > 0) z0[pt] = cf.a0 * rv;
                 if (plane_out && kcen && row >= S && row < S + TJ) {
+                    const int id = I * g.si + j * g.sj + kg;
                     r_out[id] = rv;
-                    e[id] = FIRST ? 0.f : fmaf(alpha, p[id], e[id]);
+                    e[id] = FIRST ? 0.f : fmaf(alpha, np[m], ne[m]);
                     acc_prod(arr, rv, rv);
                     if (S == 0) {
-                        const float zv = rv * A.inv_diag(id);
+                        const float zv = rv * (nc[m] == 0 ? 1.f : (A.code ? 1.f / A.k.c0 : A.inv_diag(id)));
                         z_out[id] = zv;
                         acc_prod(arz, rv, zv);
                     }
                 }
             }
+            if (I + 1 <= Iend) fetch(I + 1);
         }
         __syncthreads();
-        // ---- Chebyshev levels 1..S at plane I-lv over the tile + (S-lv) halo
+        // ---- Chebyshev levels 1..S at plane I-LV over the tile + (S-LV) halo
+        auto level = [&](auto lvc) {
+            constexpr int LV = decltype(lvc)::value;
+            const int Pk = I - LV;
+            if (Pk >= imax(0, i0 - S + LV) && Pk < imin(g.nx, i1 + S - LV) && kin && lane >= LV &&
+                lane < W - LV) {
+                const float* __restrict__ zc = zr + ((LV - 1) * 3 + Pk % 3) * PL;
+                const float* __restrict__ zw = zr + ((LV - 1) * 3 + (Pk + 2) % 3) * PL;
+                const float* __restrict__ ze = zr + ((LV - 1) * 3 + (Pk + 1) % 3) * PL;
+                const float* __restrict__ rpl = rp + (Pk % (S + 1)) * PL;
+                const uint8_t* __restrict__ crl = cr + (Pk % (S + 1)) * PL;
+                const float* __restrict__ pcp = LV >= 2 ? pcr + ((LV - 2) * 2 + Pk % 2) * PL : rpl;
+                float* __restrict__ zo = LV < S ? zr + (LV * 3 + Pk % 3) * PL : nullptr;
+                float* __restrict__ po = LV < S ? pcr + ((LV - 1) * 2 + Pk % 2) * PL : nullptr;
+                const bool out_lane = LV == S && kcen && Pk >= i0 && Pk < i1;
+                const float bk = cf.b[LV - 1], ak = cf.a[LV - 1];
+                constexpr int ITER = (H - 2 * LV + NW - 1) / NW;
 #pragma unroll
-        for (int lv = 1; lv <= S; ++lv) {
-            const int Pk = I - lv;
-            if (Pk >= imax(0, i0 - S + lv) && Pk < imin(g.nx, i1 + S - lv) && kin && lane >= lv &&
-                lane < W - lv) {
-                const float* zc = zr + ((lv - 1) * 3 + Pk % 3) * PL;
-                const float* zw = zr + ((lv - 1) * 3 + (Pk + 2) % 3) * PL;
-                const float* ze = zr + ((lv - 1) * 3 + (Pk + 1) % 3) * PL;
-                const float* rpl = rp + (Pk % (S + 1)) * PL;
-                const uint8_t* crl = cr + (Pk % (S + 1)) * PL;
-                const float* pcp = lv >= 2 ? pcr + ((lv - 2) * 2 + Pk % 2) * PL : rpl;
-                float* zo = lv < S ? zr + (lv * 3 + Pk % 3) * PL : nullptr;
-                float* po = lv < S ? pcr + ((lv - 1) * 2 + Pk % 2) * PL : nullptr;
-                const bool out_lane = lv == S && kcen && Pk >= i0 && Pk < i1;
-                for (int row = lv + warp; row < H - lv; row += NW) {
+                for (int m = 0; m < ITER; ++m) {
+                    const int row = LV + warp + m * NW;
+                    if (row >= H - LV) break;
                     const int j = j0 - S + row;
                     if (j < 0 || j >= g.ny) continue;
                     const int pt = row * W + lane;
-                    const unsigned cd = crl[pt];
                     const float zcv = zc[pt];
                     float az;
-                    if (cd == 1u) {   // all six neighbours present, base coefficients
+                    if (crl[pt] == 1u) {   // all six neighbours present, base coefficients
                         az = A.k.c0 * zcv + A.k.x1 * (zw[pt] + ze[pt]) + A.k.y1 * (zc[pt - W] + zc[pt + W]) +
                              A.k.z1 * (zc[pt - 1] + zc[pt + 1]);
                     } else {
-                        const int id = Pk * g.si + j * g.sj + kg;
-                        CoefF a = A.at(id);
-                        az = a.c * zcv;
-                        if (Pk > 0) az += a.w * zw[pt];
-                        if (Pk < g.nx - 1) az += a.e * ze[pt];
-                        if (j > 0) az += a.s * zc[pt - W];
-                        if (j < g.ny - 1) az += a.n * zc[pt + W];
-                        if (kg > 0) az += a.b * zc[pt - 1];
-                        if (kg < g.nz - 1) az += a.t * zc[pt + 1];
+                        az = az_general(A, Pk * g.si + j * g.sj + kg, Pk, j, kg, g, zc, zw, ze, pt);
                     }
                     const float rv = rpl[pt];
-                    const float pck = fmaf(cf.b[lv - 1], pcp[pt], rv - az);
-                    const float zk = fmaf(cf.a[lv - 1], pck, zcv);
-                    if (lv < S) {
+                    const float pck = fmaf(bk, pcp[pt], rv - az);
+                    const float zk = fmaf(ak, pck, zcv);
+                    if (LV < S) {
                         zo[pt] = zk;
                         po[pt] = pck;
                     } else if (out_lane && row >= S && row < S + TJ) {
@@ -263,7 +318,13 @@ __global__ void __launch_bounds__(NT) k_pass_b(Geo g, ViewF A, int CI, ChebF cf,
                 }
             }
             __syncthreads();
-        }
+        };
+        if constexpr (S >= 1) level(std::integral_constant<int, 1>{});
+        if constexpr (S >= 2) level(std::integral_constant<int, 2>{});
+        if constexpr (S >= 3) level(std::integral_constant<int, 3>{});
+        if constexpr (S >= 4) level(std::integral_constant<int, 4>{});
+        if constexpr (S >= 5) level(std::integral_constant<int, 5>{});
+        if constexpr (S >= 6) level(std::integral_constant<int, 6>{});
     }
     double v[2] = {acc_value(arr), acc_value(arz)};
     if (last_block_sum<2>(v, partials, counter, sm)) {

@@ -266,7 +266,7 @@ struct les_ctx {
     double* A[7] = {};
     bool A_valid = false;         // A[] holds the current matrix (stored, or expanded codes)
     int fused = 1;                // LES_OPT_FUSED: fused FP32 inner passes
-    int opt_tma = 1;              // LES_OPT_TMA: TMA-staged fused passes where the grid allows
+    int opt_tma = 0;              // LES_OPT_TMA: TMA-staged fused passes where the grid allows
     struct les::TmaCache* tma = nullptr;
     les::StencilCoef coef{};
     double* L[7] = {};
