@@ -62,7 +62,10 @@ def parse():
     ap.add_argument("--cpu-iters", type=int, default=12, help="PCG iterations in the CPU sample")
     ap.add_argument("--seed", type=int, default=1234)
     ap.add_argument("--inner-rtol", type=float, default=1e-4, help="mixed path: inner FP32 solve reduction")
-    ap.add_argument("--tma", type=int, default=0, help="stage the fused passes with TMA (LES_OPT_TMA)")
+    ap.add_argument("--tma", type=int, default=0, help="stage the tile passes with TMA (LES_OPT_TMA)")
+    ap.add_argument("--fused", type=int, default=1, help="inner passes: 1 register columns, 2 smem tiles, 0 unfused")
+    ap.add_argument("--rows", default="0,0", help="rows per strip of the column passes A,B (0 = built-in)")
+    ap.add_argument("--chunks", default="0,0", help="planes per march chunk of the column passes A,B (0 = auto)")
     return ap.parse_args()
 
 
@@ -126,10 +129,14 @@ class Clocks:
 
 
 # algorithmic HBM bytes per cell of one launch of each profiled kernel
-def alg_bytes_per_cell(name, degree):
-    # fused FP32 inner passes (the default): pass B reads r, q, p, e and the
-    # stencil code and writes r', e', z (the whole Chebyshev apply happens in
-    # shared memory); pass A reads z, p_old and the code and writes p, q
+def alg_bytes_per_cell(name, fused=1):
+    # fused FP32 inner passes.  Register columns (fused=1, the default): pass B
+    # reads r, q and the stencil code and writes r', z (the whole Chebyshev
+    # apply stays on chip); pass A reads z, p_old, e and the code and writes
+    # p, q, e.  Shared-memory tiles (fused=2): pass B also reads p, e and
+    # writes e; pass A reads z, p_old, code and writes p, q.
+    if fused == 1 and name in ("inner_precond_f32", "inner_spmv_f32"):
+        return {"inner_precond_f32": 17.0, "inner_spmv_f32": 25.0}[name]
     return {"inner_precond_f32": 29.0, "inner_spmv_f32": 17.0, "inner_update_f32": 28.0, "spmv_f64": 17.0,
             "update_f64": 48.0, "cheb_f64": 41.0, "outer_resid_f64": 21.0}.get(name)
 
@@ -259,7 +266,12 @@ def run_ours(args):
     shape, h, solid, f = les_cases.case(args.workload, args.seed)
     n = int(np.prod(shape))
     ctx, lmax = make_ctx(G, les_cases, shape, h, solid, f, dev, args.precond)
+    ctx.set_option(G.OPT_FUSED, args.fused)
     ctx.set_option(G.OPT_TMA, args.tma)
+    ra, rb = (int(x) for x in args.rows.split(","))
+    ca, cb = (int(x) for x in args.chunks.split(","))
+    for opt, v in ((G.OPT_ROWS_A, ra), (G.OPT_ROWS_B, rb), (G.OPT_CHUNK_A, ca), (G.OPT_CHUNK_B, cb)):
+        ctx.set_option(opt, v)
     prm = step_params(G, les_cases, args.precond, lmax, G.MIXED, args.inner_rtol)
     ctx64 = None
     if not args.no_fp64:
@@ -346,7 +358,7 @@ def run_ours(args):
     roof = None
     if prof:
         name, (cnt, ms) = max(prof.items(), key=lambda kv: kv[1][1])
-        bpc = alg_bytes_per_cell(name, 4)
+        bpc = alg_bytes_per_cell(name, args.fused)
         traffic = None
         tp = os.path.join(ROOT, "profiles", "traffic.json")
         if os.path.exists(tp):
@@ -361,7 +373,9 @@ def run_ours(args):
                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                     "alg_bytes_per_launch": bpc * n, "launches": cnt, "avg_launch_us": 1e3 * ms / cnt,
                     "share_of_step": ms / (sum(rec["ms"]) or 1.0),
-                    "kernels": {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()}}
+                    "kernels": {k: {"launches": v[0], "ms": v[1], "us_per_launch": 1e3 * v[1] / max(v[0], 1),
+                                    "gbs": (alg_bytes_per_cell(k, args.fused) or 0) * n * v[0] / max(v[1], 1e-9) / 1e6}
+                                for k, v in prof.items()}}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
@@ -371,7 +385,8 @@ def run_ours(args):
                                    (args.workload, "x".join(map(str, shape)), args.precond),
                        "cells": n, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "flushed (256 MiB write) before every timed step",
-                       "inner_rtol": args.inner_rtol, "tma": args.tma},
+                       "inner_rtol": args.inner_rtol, "tma": args.tma, "fused": args.fused,
+                       "rows": args.rows, "chunks": args.chunks},
             "e2e": e2e, "gpu_launches": launches, "wall_s": wall,
             "iters_inner_mean": statistics.mean(rec["iters"]), "outer_mean": statistics.mean(rec["outer"]),
             "rel_residual_max": max(rec["rres"]), "roofline": roof, "clocks": clk}

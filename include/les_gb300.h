@@ -221,12 +221,20 @@ les_status les_dot_noalloc(const double* a, const double* b, long long n, double
 
 /* ---- options (no reference counterpart) --------------------------------- */
 typedef enum les_option {
-    LES_OPT_FUSED = 0,  /* 1 (default): mixed-precision inner iteration as two fused
-                           passes (Jacobi, Chebyshev degree 2..7); 0: one kernel per
-                           vector operation */
-    LES_OPT_TMA = 1     /* 1: stage the fused passes' planes with TMA when nz % 16 == 0
-                           and the matrix is device-built; 0 (default): plain loads with
-                           register prefetch (higher occupancy, faster on GB300) */
+    LES_OPT_FUSED = 0,  /* mixed-precision inner iteration (Jacobi, Chebyshev degree
+                           2..7) as two fused passes: 1 (default) register-column
+                           marches (device-built matrix; stored matrices use 2);
+                           2 shared-memory tiles; 0: one kernel per vector operation */
+    LES_OPT_TMA = 1,    /* 1: the shared-memory tile passes, with their planes staged
+                           by TMA when nz % 16 == 0 and the matrix is device-built;
+                           0 (default): no TMA */
+    /* shape of the register-column passes (0 = built-in choice; les_autotune
+       sets them by timing): */
+    LES_OPT_ROWS_A = 2,   /* rows per strip of pass A: 8 or 16 */
+    LES_OPT_ROWS_B = 3,   /* rows per strip of pass B: 16 (Jacobi), 4 or 8
+                             (Chebyshev degree 2..4), 4 (degree 5..7) */
+    LES_OPT_CHUNK_A = 4,  /* planes per march chunk of pass A */
+    LES_OPT_CHUNK_B = 5   /* planes per march chunk of pass B */
 } les_option;
 les_status les_set_option(les_ctx* ctx, int option, int value);
 

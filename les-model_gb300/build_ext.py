@@ -27,6 +27,7 @@ UNITS = {
     "les_wavefront.cu": ["-fmad=false"],
     "les_mixed.cu": [],
     "les_fused.cu": [],
+    "les_col.cu": [],
     "les_step.cu": ["-fmad=false"],
     "les_noalloc.cu": ["-fmad=false"],
 }

@@ -1,0 +1,477 @@
+// les_col.cu -- the FP32 inner PCG iteration of the mixed-precision solve as
+// two register-resident column marches (Jacobi or Chebyshev preconditioner).
+//
+// Each warp owns a strip of the grid, 32 consecutive cells along k (one per
+// lane) by H rows along j, and marches along i over a chunk of planes.  A lane
+// keeps its own column of values in registers for the planes a stencil needs:
+// the i and j neighbours of a cell are registers of the same thread and the k
+// neighbours come from the adjacent lanes by warp shuffle.  There is no shared
+// memory and no block barrier inside the march; every warp runs on its own.
+//
+// Pass A (k_col_a), halo 1:
+//     p = z + beta p_old          (strip + halo)
+//     e += alpha_prev p_old       (the previous iteration's update of the inner
+//                                  solution, deferred to here so that pass B
+//                                  reads neither p nor e)
+//     q = A p, p.q -> alpha
+// Pass B (k_col_b), halo S:
+//     r' = r - alpha q, ||r'||^2
+//     z = M^-1 r': Chebyshev with S = degree-1 stencil levels (the recurrence
+//       of les-model src/pressure.cpp:871-905), temporally blocked along i --
+//       at march step I level k works on plane I-k over the strip grown by
+//       S-k cells; Jacobi (S = 0): z = r' / A_c
+//     r'.z -> beta, rho; convergence on ||r'||
+// The last p and alpha of a solve are left for col_x_update (x += e + alpha p).
+//
+// Compulsory bytes per cell and iteration: pass A reads z, p_old, e and writes
+// p, q, e (24 B); pass B reads r, q and writes r', z (16 B).
+//
+// The matrix.  These passes serve the device-built matrix of a solid-free mask
+// (the reference builds the pressure matrix before it applies the obstacle,
+// src/main.cpp:66-81), whose coefficients depend only on the position
+// (src/pressure.cpp:613-696): the base 7-point Laplacian; at the inlet plane
+// (i = 0) and at the j and k walls the missing neighbour's coefficient is
+// moved onto the opposite one (a Neumann mirror); the plane before the outlet
+// (i = nx-2) has no east coefficient; the outlet plane (i = nx-1) is an
+// identity row.  The march realises the mirrors by loading reflected
+// neighbours into the halo (row -m reads row m, plane -m reads plane m, and so
+// on): the reflected field stays mirror-symmetric through every Chebyshev
+// level, so each cell uses the interior formula and only the two outlet
+// planes need plane-uniform coefficients.  Halo cells of a strip are
+// recomputed by every strip that needs them (values of lanes and rows past
+// the shrinking halo are never used).
+#include <cmath>
+
+#include "les_internal.cuh"
+#include "les_mixed.cuh"
+
+using namespace les;
+
+namespace {
+
+constexpr int CT = 128;          // threads per block: 4 independent warps
+constexpr int CWPB = CT / 32;
+constexpr unsigned FULL = 0xffffffffu;
+
+struct Coef {
+    float c0, x1, y1, z1;
+};
+
+struct StripPos {
+    int j0;        // j of row 0
+    int i0, i1;    // owned planes [i0, i1)
+    int kl;        // this lane's k after reflection at the walls (-1: not loaded)
+    unsigned own;  // bit r: cell of row r owned by this lane
+};
+
+// reflection of index x into [0, n) about the end cells (-1 if still outside)
+__device__ __forceinline__ int reflect(int x, int n)
+{
+    x = x < 0 ? -x : x;
+    x = x > n - 1 ? 2 * (n - 1) - x : x;
+    return x >= 0 ? x : -1;
+}
+
+template <int HALO, int TJ>
+__device__ __forceinline__ StripPos strip_pos(const Geo& g, const ColMap& m, int item, int lane)
+{
+    StripPos s;
+    const int kt = item % m.tiles_k, rest = item / m.tiles_k;
+    const int jt = rest % m.tiles_j, ch = rest / m.tiles_j;
+    const int kg = kt * m.tk - HALO + lane;
+    s.j0 = jt * TJ - HALO;
+    s.i0 = ch * m.ci;
+    s.i1 = min(g.nx, s.i0 + m.ci);
+    s.kl = reflect(kg, g.nz);
+    const bool kown = kg >= 0 && kg < g.nz && lane >= HALO && lane < HALO + m.tk;
+    s.own = 0u;
+#pragma unroll
+    for (int r = HALO; r < HALO + TJ; ++r)
+        if (kown && s.j0 + r < g.ny) s.own |= 1u << r;
+    return s;
+}
+
+// offset of row r of plane P in the reflected field, or -1 (not loaded:
+// planes past the outlet are never read)
+__device__ __forceinline__ int row_off(const Geo& g, const StripPos& s, int P, int r)
+{
+    const int jl = reflect(s.j0 + r, g.ny);
+    const int pl = P < 0 ? -P : P;
+    return (jl >= 0 && s.kl >= 0 && pl < g.nx) ? pl * g.si + jl * g.sj + s.kl : -1;
+}
+
+// ---- pass A -----------------------------------------------------------------
+template <int TJ, bool FIRST>
+__global__ void __launch_bounds__(CT, TJ == 8 ? 4 : 2) k_col_a(Geo g, ColMap m, Coef k, const float* __restrict__ z,
+                                                             const float* __restrict__ pold, float* __restrict__ pnew,
+                                                             float* __restrict__ q, float* __restrict__ e,
+                                                             double* partials, unsigned* counter, SolverState* st,
+                                                             int pslot)
+{
+    constexpr int H = TJ + 2;
+    __shared__ double sm[32];
+    if (st->done) return;
+    const float beta = FIRST ? 0.f : (float)st->beta;
+    const float aprev = FIRST ? 0.f : (float)st->alpha;
+    const int lane = threadIdx.x & 31;
+    const int item = blockIdx.x * CWPB + (threadIdx.x >> 5);
+    Acc acc;
+    if (item < m.items) {
+        const StripPos s = strip_pos<1, TJ>(g, m, item, lane);
+        float p0[H], p1[H], p2[H];   // p at planes P, P-1, P-2
+        float vz[H], vp[H], ve[TJ];  // z, p_old, e of the plane being fetched
+#pragma unroll
+        for (int r = 0; r < H; ++r) p0[r] = p1[r] = p2[r] = 0.f;
+        auto fetch = [&](int P) {
+            const bool pown = P >= s.i0 && P < s.i1;
+#pragma unroll
+            for (int r = 0; r < H; ++r) {
+                const int id = row_off(g, s, P, r);
+                vz[r] = id >= 0 ? z[id] : 0.f;
+                vp[r] = (!FIRST && id >= 0) ? pold[id] : 0.f;
+                if (r >= 1 && r <= TJ) ve[r - 1] = (!FIRST && pown && ((s.own >> r) & 1u)) ? e[id] : 0.f;
+            }
+        };
+        fetch(s.i0 - 1);
+        for (int P = s.i0 - 1; P <= s.i1; ++P) {
+#pragma unroll
+            for (int r = 0; r < H; ++r) p0[r] = FIRST ? vz[r] : fmaf(beta, vp[r], vz[r]);
+            if (P >= s.i0 && P < s.i1) {
+                const int base = P * g.si + s.j0 * g.sj + s.kl;   // owned cells: no reflection
+#pragma unroll
+                for (int r = 1; r <= TJ; ++r) {
+                    if ((s.own >> r) & 1u) {
+                        const int id = base + r * g.sj;
+                        pnew[id] = p0[r];
+                        e[id] = FIRST ? 0.f : fmaf(aprev, vp[r], ve[r - 1]);
+                    }
+                }
+            }
+            if (P < s.i1) fetch(P + 1);
+            // q = A p at plane C = P - 1
+            const int C = P - 1;
+            if (C >= s.i0) {
+                const int cb = C * g.si + s.j0 * g.sj + s.kl;
+                const bool ident = C == g.nx - 1;           // outlet plane: identity row
+                const float ex = C == g.nx - 2 ? 0.f : k.x1; // no east coefficient before the outlet
+                float sq = 0.f;
+#pragma unroll
+                for (int r = 1; r <= TJ; ++r) {
+                    const float pc = p1[r];
+                    const float pb = __shfl_up_sync(FULL, pc, 1);
+                    const float pt = __shfl_down_sync(FULL, pc, 1);
+                    if ((s.own >> r) & 1u) {
+                        float val = k.c0 * pc + k.x1 * p2[r] + ex * p0[r] + k.y1 * (p1[r - 1] + p1[r + 1]) +
+                                    k.z1 * (pb + pt);
+                        val = ident ? pc : val;
+                        q[cb + r * g.sj] = val;
+                        sq = fmaf(pc, val, sq);
+                    }
+                }
+                acc_add(acc, sq);
+            }
+#pragma unroll
+            for (int r = 0; r < H; ++r) {
+                p2[r] = p1[r];
+                p1[r] = p0[r];
+            }
+        }
+    }
+    double v[1] = {acc_value(acc)};
+    if (last_block_sum<1>(v, partials, counter, sm)) {
+        if (threadIdx.x == 0) {
+            st->alpha = st->rho / v[0];
+            st->buf = pslot;   // buffer holding this iteration's p
+        }
+    }
+}
+
+// ---- pass B -----------------------------------------------------------------
+template <int S, int TJ, bool FIRST>
+__global__ void __launch_bounds__(CT, (TJ == 4 && S <= 3) ? 3 : 2) k_col_b(Geo g, ColMap m, Coef k, ChebF cf, float inv_c0,
+                                               const float* __restrict__ r_in, float* __restrict__ r_out,
+                                               const float* __restrict__ q, float* __restrict__ z_out,
+                                               double* partials, unsigned* counter, SolverState* st,
+                                               SolverState* outer, int total_cap)
+{
+    constexpr int H = TJ + 2 * S;
+    constexpr int NL = S > 1 ? S - 1 : 1;   // stored levels z_1 .. z_{S-1}
+    __shared__ double sm[64];
+    if (st->done) return;
+    const float alpha = FIRST ? 0.f : (float)st->alpha;
+    const int lane = threadIdx.x & 31;
+    const int item = blockIdx.x * CWPB + (threadIdx.x >> 5);
+    Acc arr, arz;
+    if (item < m.items) {
+        const StripPos s = strip_pos<S, TJ>(g, m, item, lane);
+        float rp[S + 1][H];      // r' at planes I - d
+        float zr[NL][3][H];      // z_L at planes I - L - d (L = 1 .. S-1 at [L-1])
+        float pcr[NL][2][H];     // pc_L at planes I - L - d
+        float vr[H], vq[H];      // r, q of the plane being fetched
+#pragma unroll
+        for (int d = 0; d <= S; ++d)
+#pragma unroll
+            for (int r = 0; r < H; ++r) rp[d][r] = 0.f;
+#pragma unroll
+        for (int L = 0; L < NL; ++L)
+#pragma unroll
+            for (int r = 0; r < H; ++r) {
+                zr[L][0][r] = zr[L][1][r] = zr[L][2][r] = 0.f;
+                pcr[L][0][r] = pcr[L][1][r] = 0.f;
+            }
+        auto fetch = [&](int P) {
+#pragma unroll
+            for (int r = 0; r < H; ++r) {
+                const int id = row_off(g, s, P, r);
+                vr[r] = id >= 0 ? r_in[id] : 0.f;
+                vq[r] = (!FIRST && id >= 0) ? q[id] : 0.f;
+            }
+        };
+        fetch(s.i0 - S);
+        for (int I = s.i0 - S; I < s.i1 + S; ++I) {
+            // ---- level 0 at plane I
+            {
+                const bool pown = I >= s.i0 && I < s.i1;
+                const int base = I * g.si + s.j0 * g.sj + s.kl;
+                const float dinv = I == g.nx - 1 ? 1.f : inv_c0;   // Jacobi: identity row at the outlet
+                float srr = 0.f, srz = 0.f;
+#pragma unroll
+                for (int r = 0; r < H; ++r) {
+                    const float rv = FIRST ? vr[r] : fmaf(-alpha, vq[r], vr[r]);
+                    rp[0][r] = rv;
+                    if (pown && ((s.own >> r) & 1u)) {
+                        const int id = base + r * g.sj;
+                        r_out[id] = rv;
+                        srr = fmaf(rv, rv, srr);
+                        if (S == 0) {
+                            const float zv = rv * dinv;
+                            z_out[id] = zv;
+                            srz = fmaf(rv, zv, srz);
+                        }
+                    }
+                }
+                if (pown) {
+                    acc_add(arr, srr);
+                    if (S == 0) acc_add(arz, srz);
+                }
+            }
+            if (I + 1 < s.i1 + S) fetch(I + 1);
+            // ---- Chebyshev levels 1..S at planes I-1 .. I-S
+#pragma unroll
+            for (int LV = 1; LV <= S; ++LV) {
+                const int Pk = I - LV;
+                const float ak = cf.a[LV - 1], bk = cf.b[LV - 1];
+                const bool ident = Pk == g.nx - 1;
+                const float ex = Pk == g.nx - 2 ? 0.f : k.x1;
+                const bool out_plane = LV == S && Pk >= s.i0 && Pk < s.i1;
+                const int pbase = Pk * g.si + s.j0 * g.sj + s.kl;
+                float s2 = 0.f;
+#pragma unroll
+                for (int r = LV; r < H - LV; ++r) {
+                    float zc, zw, ze, zs, zn, pcp;
+                    if (LV == 1) {   // z_0 = a0 r', pc_0 = r'
+                        zc = rp[1][r]; zw = rp[2][r]; ze = rp[0][r];
+                        zs = rp[1][r - 1]; zn = rp[1][r + 1];
+                        pcp = rp[1][r];
+                    } else {
+                        zc = zr[LV - 2][1][r]; zw = zr[LV - 2][2][r]; ze = zr[LV - 2][0][r];
+                        zs = zr[LV - 2][1][r - 1]; zn = zr[LV - 2][1][r + 1];
+                        pcp = pcr[LV - 2][1][r];
+                    }
+                    const float zb = __shfl_up_sync(FULL, zc, 1);
+                    const float zt = __shfl_down_sync(FULL, zc, 1);
+                    float az = k.c0 * zc + k.x1 * zw + ex * ze + k.y1 * (zs + zn) + k.z1 * (zb + zt);
+                    az = ident ? zc : az;
+                    if (LV == 1) {
+                        az *= cf.a0;
+                        zc *= cf.a0;
+                    }
+                    const float rv = rp[LV][r];
+                    const float pck = fmaf(bk, pcp, rv - az);
+                    const float zk = fmaf(ak, pck, zc);
+                    if (LV < S) {
+                        zr[LV - 1][0][r] = zk;
+                        pcr[LV - 1][0][r] = pck;
+                    } else if (out_plane && ((s.own >> r) & 1u)) {
+                        z_out[pbase + r * g.sj] = zk;
+                        s2 = fmaf(rv, zk, s2);
+                    }
+                }
+                if (out_plane) acc_add(arz, s2);
+            }
+            // ---- rotate the rings by one plane
+#pragma unroll
+            for (int d = S; d >= 1; --d)
+#pragma unroll
+                for (int r = 0; r < H; ++r) rp[d][r] = rp[d - 1][r];
+#pragma unroll
+            for (int L = 0; L < S - 1; ++L)
+#pragma unroll
+                for (int r = 0; r < H; ++r) {
+                    zr[L][2][r] = zr[L][1][r];
+                    zr[L][1][r] = zr[L][0][r];
+                    pcr[L][1][r] = pcr[L][0][r];
+                }
+        }
+    }
+    double v[2] = {acc_value(arr), acc_value(arz)};
+    if (last_block_sum<2>(v, partials, counter, sm)) {
+        if (threadIdx.x == 0) {
+            if (FIRST) {
+                st->rho = v[1];
+            } else {
+                const double err = sqrt(v[0]);
+                const int kk = st->k + 1;
+                st->k = kk;
+                st->err = err;
+                const int total = outer->iters + 1;
+                outer->iters = total;
+                if (err < st->tol) { st->done = 1; st->status = LES_OK; }
+                else if (!isfinite(err)) { st->done = 1; st->status = LES_NONFINITE; }
+                else if (kk >= st->max_iter || total >= total_cap) { st->done = 1; st->status = LES_NOT_CONVERGED; }
+                st->beta = v[1] / st->rho;
+                st->rho = v[1];
+            }
+        }
+    }
+}
+
+// x += e + alpha p_last (FP64 solution, FP32 correction)
+__global__ void k_x_update(Geo g, double* __restrict__ x, const float* __restrict__ e, const float* __restrict__ p0,
+                           const float* __restrict__ p1, const SolverState* in)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.n) return;
+    const float a = (float)in->alpha;
+    const float* p = in->buf ? p1 : p0;
+    x[t] = __dadd_rn(x[t], (double)fmaf(a, p[t], e[t]));
+}
+
+// ---- launch plumbing ----------------------------------------------------------
+using KA = void (*)(Geo, ColMap, Coef, const float*, const float*, float*, float*, float*, double*, unsigned*,
+                    SolverState*, int);
+using KB = void (*)(Geo, ColMap, Coef, ChebF, float, const float*, float*, const float*, float*, double*, unsigned*,
+                    SolverState*, SolverState*, int);
+
+KA pick_a(int tj, bool first)
+{
+    if (tj == 8) return first ? k_col_a<8, true> : k_col_a<8, false>;
+    return first ? k_col_a<16, true> : k_col_a<16, false>;
+}
+
+// (levels, rows) instantiated: Jacobi 16 rows; 1..3 levels 4 or 8 rows;
+// 4..6 levels 4 rows
+KB pick_b(int S, int tj, bool first)
+{
+#define LES_B(s, t) return first ? k_col_b<s, t, true> : k_col_b<s, t, false>
+    switch (S) {
+    case 0: LES_B(0, 16);
+    case 1: if (tj == 4) LES_B(1, 4); LES_B(1, 8);
+    case 2: if (tj == 4) LES_B(2, 4); LES_B(2, 8);
+    case 3: if (tj == 4) LES_B(3, 4); LES_B(3, 8);
+    case 4: LES_B(4, 4);
+    case 5: LES_B(5, 4);
+    default: LES_B(6, 4);
+    }
+#undef LES_B
+}
+
+int default_tj_b(int S) { return S == 0 ? 16 : (S <= 3 ? 8 : 4); }
+
+bool valid_tj_b(int S, int tj)
+{
+    if (S == 0) return tj == 16;
+    if (S <= 3) return tj == 4 || tj == 8;
+    return tj == 4;
+}
+
+// Strips x chunks for one pass: as many chunks along i as fit in one wave of
+// resident warps (a partial second wave would double the pass time); a
+// chunk re-reads 2 x halo planes.
+ColMap col_map(les_ctx* c, const void* fn, int halo, int tj, int ci_force)
+{
+    const Geo& g = c->g;
+    ColMap m{};
+    m.tk = 32 - 2 * halo;
+    m.tj = tj;
+    m.tiles_k = (g.nz + m.tk - 1) / m.tk;
+    m.tiles_j = (g.ny + tj - 1) / tj;
+    const int tiles = m.tiles_k * m.tiles_j;
+    int ci = ci_force;
+    if (ci <= 0) {
+        int occ = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, CT, 0);
+        const long long warps = (long long)(occ < 1 ? 1 : occ) * CWPB * c->sms;
+        long long chunks = warps / tiles;
+        if (chunks < 1) chunks = 1;
+        ci = (int)((g.nx + chunks - 1) / chunks);
+        const int min_ci = 2 * halo > 4 ? 2 * halo : 4;
+        if (ci < min_ci) ci = min_ci;
+    }
+    if (ci > g.nx) ci = g.nx;
+    m.ci = ci;
+    m.items = tiles * ((g.nx + ci - 1) / ci);
+    return m;
+}
+
+}  // namespace
+
+namespace les {
+
+bool col_supported(const les_ctx* c, const les_pcg_opts* o)
+{
+    if (!(c->fused == 1 && !c->opt_tma && c->stencil_mode == 1 && c->code_plain && fused_supported(o))) return false;
+    // the reflections need the mirrored rows, columns and planes inside the grid
+    const int S = o->precond == LES_PC_JACOBI ? 1 : (o->degree - 1 > 1 ? o->degree - 1 : 1);
+    const Geo& g = c->g;
+    return g.nx >= 2 * S + 4 && g.ny >= 2 * S + 2 && g.nz >= 2 * S + 2;
+}
+
+les_status col_plan(les_ctx* c, const les_pcg_opts* o, ViewF A, SolverState* in, SolverState* out, ColPlan& P)
+{
+    P.S = o->precond == LES_PC_JACOBI ? 0 : o->degree - 1;
+    P.cf = cheb_coefs(o);
+    P.inv_c0 = 1.f / A.k.c0;
+    P.A = A;
+    P.in = in;
+    P.out = out;
+    P.cap = o->max_iter;
+    const int tja = (c->tune_tja == 8 || c->tune_tja == 16) ? c->tune_tja : 8;
+    const int tjb = valid_tj_b(P.S, c->tune_tjb) ? c->tune_tjb : default_tj_b(P.S);
+    P.ma = col_map(c, (const void*)pick_a(tja, false), 1, tja, c->tune_cia);
+    P.mb = col_map(c, (const void*)pick_b(P.S, tjb, false), P.S, tjb, c->tune_cib);
+    P.blocks_a = (P.ma.items + CWPB - 1) / CWPB;
+    P.blocks_b = (P.mb.items + CWPB - 1) / CWPB;
+    if ((size_t)2 * P.blocks_a > c->partials_len || (size_t)2 * P.blocks_b > c->partials_len)
+        return fail(c, LES_BAD_ARG, "column pass grid exceeds the reduction scratch");
+    return LES_OK;
+}
+
+static Coef coef_of(const ColPlan& P) { return Coef{P.A.k.c0, P.A.k.x1, P.A.k.y1, P.A.k.z1}; }
+
+les_status col_pass_a(les_ctx* c, const ColPlan& P, bool first, int pc)
+{
+    float *z = c->f[1], *pb[2] = {c->f[2], c->f[3]}, *q = c->f[4], *e = c->f[5];
+    launch_p(c, PROF_IN_SPMV, pick_a(P.ma.tj, first), P.blocks_a, CT, c->g, P.ma, coef_of(P), (const float*)z,
+             (const float*)pb[pc], pb[pc ^ 1], q, e, c->partials, c->counters + 15, P.in, pc ^ 1);
+    return check_launch(c, "column pass A");
+}
+
+les_status col_pass_b(les_ctx* c, const ColPlan& P, bool first, int rin)
+{
+    float* r[2] = {c->f[0], c->f[6]};
+    float *z = c->f[1], *q = c->f[4];
+    launch_p(c, PROF_IN_CHEB, pick_b(P.S, P.mb.tj, first), P.blocks_b, CT, c->g, P.mb, coef_of(P), P.cf, P.inv_c0,
+             (const float*)r[rin], r[rin ^ 1], (const float*)q, z, c->partials, c->counters + 14, P.in, P.out, P.cap);
+    return check_launch(c, "column pass B");
+}
+
+les_status col_x_update(les_ctx* c)
+{
+    const Geo& g = c->g;
+    launch(c, k_x_update, (g.n + 255) / 256, 256, g, c->slot[LES_P], (const float*)c->f[5], (const float*)c->f[2],
+           (const float*)c->f[3], (const SolverState*)(c->state + 1));
+    return check_launch(c, "solution update");
+}
+
+}  // namespace les

@@ -336,8 +336,12 @@ les_status les_set_option(les_ctx* c, int option, int value)
 {
     if (!c) return LES_BAD_ARG;
     switch (option) {
-    case LES_OPT_FUSED: c->fused = value ? 1 : 0; return LES_OK;
+    case LES_OPT_FUSED: c->fused = value == 2 ? 2 : (value ? 1 : 0); return LES_OK;
     case LES_OPT_TMA: c->opt_tma = value ? 1 : 0; return LES_OK;
+    case LES_OPT_ROWS_A: c->tune_tja = value; return LES_OK;
+    case LES_OPT_ROWS_B: c->tune_tjb = value; return LES_OK;
+    case LES_OPT_CHUNK_A: c->tune_cia = value < 0 ? 0 : value; return LES_OK;
+    case LES_OPT_CHUNK_B: c->tune_cib = value < 0 ? 0 : value; return LES_OK;
     default: return fail(c, LES_BAD_ARG, "unknown option");
     }
 }

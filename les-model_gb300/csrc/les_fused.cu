@@ -37,30 +37,6 @@ constexpr int NT = 256;   // 8 warps
 constexpr int NW = NT / 32;
 constexpr int W = 32;     // shared-memory row width
 
-// double-float accumulator: the sum is hi + lo
-struct Acc {
-    float hi = 0.f, lo = 0.f;
-};
-
-__device__ __forceinline__ void acc_add(Acc& a, float x)
-{
-    float s = __fadd_rn(a.hi, x);
-    float bp = __fsub_rn(s, a.hi);
-    float err = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bp)), __fsub_rn(x, bp));
-    a.hi = s;
-    a.lo = __fadd_rn(a.lo, err);
-}
-
-__device__ __forceinline__ void acc_prod(Acc& a, float x, float y)
-{
-    float p = __fmul_rn(x, y);
-    float pe = __fmaf_rn(x, y, -p);   // exact low part of x*y
-    acc_add(a, p);
-    a.lo = __fadd_rn(a.lo, pe);
-}
-
-__device__ __forceinline__ double acc_value(const Acc& a) { return (double)a.hi + (double)a.lo; }
-
 __device__ __forceinline__ int imin(int a, int b) { return a < b ? a : b; }
 __device__ __forceinline__ int imax(int a, int b) { return a > b ? a : b; }
 
@@ -172,11 +148,6 @@ __global__ void __launch_bounds__(NT, 6) k_pass_a(Geo g, ViewF A, int CI, const 
 }
 
 // ---- pass B -----------------------------------------------------------------
-struct ChebF {
-    float a0;
-    float a[8], b[8];
-};
-
 template <int S>
 struct BGeom {
     static constexpr int TK = W - 2 * S;   // output columns
@@ -783,6 +754,25 @@ static bool build_tma(les_ctx* c, int S)
     return ok;
 }
 
+ChebF cheb_coefs(const les_pcg_opts* o)
+{
+    ChebF cf{};
+    const int S = o->precond == LES_PC_CHEBYSHEV ? o->degree - 1 : 0;
+    if (S > 0) {
+        const double d = (o->lambda_max + o->lambda_min) / 2.0;
+        const double cc = (o->lambda_max - o->lambda_min) / 2.0;
+        double alpha = 2.0 / d;
+        cf.a0 = (float)alpha;
+        for (int k = 1; k <= S && k <= 8; ++k) {
+            const double beta = (cc * alpha / 2.0) * (cc * alpha / 2.0);
+            alpha = 1.0 / (d - beta);
+            cf.a[k - 1] = (float)alpha;
+            cf.b[k - 1] = (float)beta;
+        }
+    }
+    return cf;
+}
+
 bool fused_supported(const les_pcg_opts* o)
 {
     if (o->precond == LES_PC_JACOBI) return true;
@@ -791,31 +781,43 @@ bool fused_supported(const les_pcg_opts* o)
 
 // One inner FP32 solve A e = r (e from 0) with the fused passes.  f[0] holds
 // the right-hand side on entry and is used as scratch.
-les_status inner_solve_fused(les_ctx* c, const les_pcg_opts* o, ViewF A, SolverState* in, SolverState* out,
-                             int inner_cap)
+// Everything a launch of the fused passes needs, fixed for one solve (and
+// baked into a captured graph).
+struct FusedPlan {
+    bool col = false;   // register-column passes (les_col.cu) instead of the tiles below
+    ColPlan cp;
+    int S = 0;
+    ChebF cf{};
+    bool tma = false;
+    size_t smem_b = 0;
+    const void* fb[2] = {};
+    int CIA = 8, CIB = 8;
+    dim3 ga, gb;
+    ViewF A{};
+    SolverState* in = nullptr;
+    SolverState* out = nullptr;
+    int cap = 0;
+};
+
+les_status fused_plan(les_ctx* c, const les_pcg_opts* o, ViewF A, SolverState* in, SolverState* out, FusedPlan& P)
 {
     const Geo& g = c->g;
     const int S = o->precond == LES_PC_JACOBI ? 0 : o->degree - 1;
-    ChebF cf{};
-    if (S > 0) {
-        const double d = (o->lambda_max + o->lambda_min) / 2.0;
-        const double cc = (o->lambda_max - o->lambda_min) / 2.0;
-        double alpha = 2.0 / d;
-        cf.a0 = (float)alpha;
-        for (int k = 1; k <= S; ++k) {
-            const double beta = (cc * alpha / 2.0) * (cc * alpha / 2.0);
-            alpha = 1.0 / (d - beta);
-            cf.a[k - 1] = (float)alpha;
-            cf.b[k - 1] = (float)beta;
-        }
+    if (col_supported(c, o)) {
+        P.col = true;
+        return col_plan(c, o, A, in, out, P.cp);
     }
-    float* r[2] = {c->f[0], c->f[6]};
-    float *z = c->f[1], *pb[2] = {c->f[2], c->f[3]}, *q = c->f[4], *e = c->f[5];
+    P.S = S;
+    P.A = A;
+    P.in = in;
+    P.out = out;
+    P.cap = o->max_iter;
+    P.cf = cheb_coefs(o);
     const bool tma = c->opt_tma && build_tma(c, S);
-
+    P.tma = tma;
     size_t smem_b = 0;
     int tk_b = W, tj_b = 16;
-    const void* fb[2] = {};
+    const void** fb = P.fb;
     switch (S) {
 #define LES_CASE(s)                                                                              \
     case s:                                                                                      \
@@ -828,74 +830,95 @@ les_status inner_solve_fused(les_ctx* c, const les_pcg_opts* o, ViewF A, SolverS
     default: LES_CASE(6)
 #undef LES_CASE
     }
+    P.smem_b = smem_b;
     if (smem_b > 48 * 1024)
-        for (auto f : fb) {
-            les_status st = check_cuda(c, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b),
-                                       "smem attribute");
+        for (int q = 0; q < 2; ++q) {
+            les_status st = check_cuda(
+                c, cudaFuncSetAttribute(fb[q], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b), "smem attribute");
             if (st) return st;
         }
     const int tiles_a = ((g.nz + A_TK - 1) / A_TK) * ((g.ny + A_TJ - 1) / A_TJ);
     const int tiles_b = ((g.nz + tk_b - 1) / tk_b) * ((g.ny + tj_b - 1) / tj_b);
     const void* fa = tma ? (const void*)k_pass_a_tma<false> : (const void*)k_pass_a<false>;
-    const int CIA = chunk_len(c, fa, 0, tiles_a, 8);
-    const int CIB = chunk_len(c, fb[1], smem_b, tiles_b, 4 * S > 8 ? 4 * S : 8);
-    const dim3 ga((g.nz + A_TK - 1) / A_TK, (g.ny + A_TJ - 1) / A_TJ, (g.nx + CIA - 1) / CIA);
-    const dim3 gb((g.nz + tk_b - 1) / tk_b, (g.ny + tj_b - 1) / tj_b, (g.nx + CIB - 1) / CIB);
+    P.CIA = c->tune_cia > 0 ? c->tune_cia : chunk_len(c, fa, 0, tiles_a, 8);
+    P.CIB = (c->tune_cib > 0 && c->tune_s == S) ? c->tune_cib : chunk_len(c, fb[1], smem_b, tiles_b, 4 * S > 8 ? 4 * S : 8);
+    P.ga = dim3((g.nz + A_TK - 1) / A_TK, (g.ny + A_TJ - 1) / A_TJ, (g.nx + P.CIA - 1) / P.CIA);
+    P.gb = dim3((g.nz + tk_b - 1) / tk_b, (g.ny + tj_b - 1) / tj_b, (g.nx + P.CIB - 1) / P.CIB);
+    return LES_OK;
+}
 
-    auto pass_b = [&](bool first, int rin, int pcur) -> les_status {
-        if (!tma) {
-            switch (S) {
-            case 0: return launch_b<0>(c, first, CIB, A, cf, r[rin], r[rin ^ 1], q, pb[pcur], e, z, in, out, o->max_iter);
-            case 1: return launch_b<1>(c, first, CIB, A, cf, r[rin], r[rin ^ 1], q, pb[pcur], e, z, in, out, o->max_iter);
-            case 2: return launch_b<2>(c, first, CIB, A, cf, r[rin], r[rin ^ 1], q, pb[pcur], e, z, in, out, o->max_iter);
-            case 3: return launch_b<3>(c, first, CIB, A, cf, r[rin], r[rin ^ 1], q, pb[pcur], e, z, in, out, o->max_iter);
-            case 4: return launch_b<4>(c, first, CIB, A, cf, r[rin], r[rin ^ 1], q, pb[pcur], e, z, in, out, o->max_iter);
-            case 5: return launch_b<5>(c, first, CIB, A, cf, r[rin], r[rin ^ 1], q, pb[pcur], e, z, in, out, o->max_iter);
-            default: return launch_b<6>(c, first, CIB, A, cf, r[rin], r[rin ^ 1], q, pb[pcur], e, z, in, out, o->max_iter);
-            }
-        }
+// Pass A: p_new = pb[pc^1] from z and p_old = pb[pc].
+les_status emit_pass_a(les_ctx* c, const FusedPlan& P, bool first, int pc)
+{
+    if (P.col) return col_pass_a(c, P.cp, first, pc);
+    float *z = c->f[1], *pb[2] = {c->f[2], c->f[3]}, *q = c->f[4];
+    if (P.tma) {
         const TmaCache& t = *c->tma;
-        cudaEvent_t e1 = nullptr;
-        if (c->prof_on) prof_begin(c, PROF_IN_CHEB, &e1);
-        const void* fn = fb[first ? 0 : 1];
-        float* rout = r[rin ^ 1];
-        double* parts = c->partials;
-        unsigned* cnt = c->counters + 14;
-        int CI = CIB, cap = o->max_iter;
-        Geo gg = g;
-        ViewF AA = A;
-        ChebF cff = cf;
-        void* args[] = {&gg, &AA, &CI, &cff, (void*)&t.b_r[rin], (void*)&t.b_q, (void*)&t.b_c, (void*)&t.b_e,
-                        (void*)&t.b_p[pcur], &rout, &e, &z, &parts, &cnt, &in, &out, &cap};
-        les_status st = check_cuda(c, cudaLaunchKernel(fn, gb, dim3(NT), args, smem_b, c->stream), "pass B (TMA)");
-        ++c->launches;
-        if (e1) cudaEventRecord(e1, c->stream);
-        return st;
-    };
-    les_status st = pass_b(true, 0, 0);   // z = M^-1 r, rho, e = 0
+        auto ka = first ? k_pass_a_tma<true> : k_pass_a_tma<false>;
+        launch_p(c, PROF_IN_SPMV, ka, P.ga, dim3(NT), c->g, P.A, P.CIA, t.a_z, t.a_p[pc], t.a_c, pb[pc ^ 1], q,
+                 c->partials, c->counters + 15, P.in);
+    } else {
+        auto ka = first ? k_pass_a<true> : k_pass_a<false>;
+        launch_p(c, PROF_IN_SPMV, ka, P.ga, dim3(NT), c->g, P.A, P.CIA, (const float*)z, (const float*)pb[pc],
+                 pb[pc ^ 1], q, c->partials, c->counters + 15, P.in);
+    }
+    return check_launch(c, "pass A");
+}
+
+// Pass B: r[rin] -> r[rin^1], p = pb[pcur].
+les_status emit_pass_b(les_ctx* c, const FusedPlan& P, bool first, int rin, int pcur)
+{
+    if (P.col) return col_pass_b(c, P.cp, first, rin);
+    float* r[2] = {c->f[0], c->f[6]};
+    float *z = c->f[1], *pb[2] = {c->f[2], c->f[3]}, *q = c->f[4], *e = c->f[5];
+    if (!P.tma) {
+        switch (P.S) {
+        case 0: return launch_b<0>(c, first, P.CIB, P.A, P.cf, r[rin], r[rin ^ 1], q, pb[pcur], e, z, P.in, P.out, P.cap);
+        case 1: return launch_b<1>(c, first, P.CIB, P.A, P.cf, r[rin], r[rin ^ 1], q, pb[pcur], e, z, P.in, P.out, P.cap);
+        case 2: return launch_b<2>(c, first, P.CIB, P.A, P.cf, r[rin], r[rin ^ 1], q, pb[pcur], e, z, P.in, P.out, P.cap);
+        case 3: return launch_b<3>(c, first, P.CIB, P.A, P.cf, r[rin], r[rin ^ 1], q, pb[pcur], e, z, P.in, P.out, P.cap);
+        case 4: return launch_b<4>(c, first, P.CIB, P.A, P.cf, r[rin], r[rin ^ 1], q, pb[pcur], e, z, P.in, P.out, P.cap);
+        case 5: return launch_b<5>(c, first, P.CIB, P.A, P.cf, r[rin], r[rin ^ 1], q, pb[pcur], e, z, P.in, P.out, P.cap);
+        default: return launch_b<6>(c, first, P.CIB, P.A, P.cf, r[rin], r[rin ^ 1], q, pb[pcur], e, z, P.in, P.out, P.cap);
+        }
+    }
+    const TmaCache& t = *c->tma;
+    cudaEvent_t e1 = nullptr;
+    if (c->prof_on) prof_begin(c, PROF_IN_CHEB, &e1);
+    const void* fn = P.fb[first ? 0 : 1];
+    float* rout = r[rin ^ 1];
+    double* parts = c->partials;
+    unsigned* cnt = c->counters + 14;
+    int CI = P.CIB, cap = P.cap;
+    Geo gg = c->g;
+    ViewF AA = P.A;
+    ChebF cff = P.cf;
+    SolverState *in = P.in, *out = P.out;
+    void* args[] = {&gg, &AA, &CI, &cff, (void*)&t.b_r[rin], (void*)&t.b_q, (void*)&t.b_c, (void*)&t.b_e,
+                    (void*)&t.b_p[pcur], &rout, &e, &z, &parts, &cnt, &in, &out, &cap};
+    les_status st = check_cuda(c, cudaLaunchKernel(fn, P.gb, dim3(NT), args, P.smem_b, c->stream), "pass B (TMA)");
+    ++c->launches;
+    if (e1) cudaEventRecord(e1, c->stream);
+    return st;
+}
+
+les_status inner_solve_fused(les_ctx* c, const les_pcg_opts* o, ViewF A, SolverState* in, SolverState* out,
+                             int inner_cap)
+{
+    FusedPlan P;
+    les_status st = fused_plan(c, o, A, in, out, P);
+    if (st) return st;
+    st = emit_pass_b(c, P, true, 0, 0);   // z = M^-1 r, rho, e = 0
     if (st) return st;
     int rc = 1, pc = 0, launched = 0, batch = 4;
     for (;;) {
         for (int it = 0; it < batch; ++it) {
-            const bool first = launched + it == 0;
-            if (tma) {
-                const TmaCache& t = *c->tma;
-                auto ka = first ? k_pass_a_tma<true> : k_pass_a_tma<false>;
-                launch_p(c, PROF_IN_SPMV, ka, ga, dim3(NT), g, A, CIA, t.a_z, t.a_p[pc], t.a_c, pb[pc ^ 1], q,
-                         c->partials, c->counters + 15, in);
-            } else {
-                auto ka = first ? k_pass_a<true> : k_pass_a<false>;
-                launch_p(c, PROF_IN_SPMV, ka, ga, dim3(NT), g, A, CIA, (const float*)z, (const float*)pb[pc],
-                         pb[pc ^ 1], q, c->partials, c->counters + 15, in);
-            }
+            if ((st = emit_pass_a(c, P, launched + it == 0, pc))) return st;
             pc ^= 1;
-            st = pass_b(false, rc, pc);
-            if (st) return st;
+            if ((st = emit_pass_b(c, P, false, rc, pc))) return st;
             rc ^= 1;
         }
         launched += batch;
-        st = check_launch(c, "fused inner iteration");
-        if (st) return st;
         st = read_state(c);
         if (st) return st;
         if (c->h_state[1].done || launched >= inner_cap) break;
@@ -903,6 +926,114 @@ les_status inner_solve_fused(les_ctx* c, const les_pcg_opts* o, ViewF A, SolverS
     }
     if (c->h_state[1].status == LES_TIMEOUT) return fail(c, LES_TIMEOUT, "a TMA wait in the inner solve timed out");
     return LES_OK;
+}
+
+// ---- the whole mixed solve as a CUDA graph -----------------------------------
+// Both loops run on the device: each is a conditional `while` node whose body
+// ends with a one-thread kernel that sets the loop's condition from the
+// solver state.  The inner body holds two iterations so that the ping-pong
+// buffers are in the same roles every time it repeats (kernels of an
+// iteration that starts after convergence exit at once).
+
+__global__ void k_cond_inner(const SolverState* in, cudaGraphConditionalHandle h, int cap)
+{
+    cudaGraphSetConditional(h, (!in->done && in->k < cap) ? 1u : 0u);
+}
+
+__global__ void k_cond_outer(const SolverState* out, cudaGraphConditionalHandle h, int max_outer, int cap)
+{
+    cudaGraphSetConditional(h, (!out->done && out->k < max_outer && out->iters < cap) ? 1u : 0u);
+}
+
+// Adds a `while` loop at the current capture point of c->stream: creates the
+// loop's condition handle, captures `entry(h)` (a kernel that sets the
+// condition from the solver state, so the loop can be skipped and is
+// re-armed each time an enclosing loop comes back to it), adds the
+// conditional node, captures its body with `body(h)` (which must end by
+// setting the condition again), and resumes the capture after the node.
+template <class Entry, class Body>
+static les_status capture_while(les_ctx* c, Entry entry, Body body)
+{
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    les_status st = check_cuda(c, cudaStreamGetCaptureInfo(c->stream, &cs, nullptr, &g, &deps, nullptr, &ndeps),
+                               "capture info");
+    if (st) return st;
+    if (cs != cudaStreamCaptureStatusActive) return fail(c, LES_BAD_ARG, "internal: not capturing");
+    cudaGraphConditionalHandle h;
+    st = check_cuda(c, cudaGraphConditionalHandleCreate(&h, g, 0, 0), "conditional handle");
+    if (st) return st;
+    if ((st = entry(h))) return st;
+    st = check_cuda(c, cudaStreamGetCaptureInfo(c->stream, &cs, nullptr, &g, &deps, nullptr, &ndeps), "capture info");
+    if (st) return st;
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    st = check_cuda(c, cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &np), "conditional node");
+    if (st) return st;
+    cudaGraph_t bodyg = np.conditional.phGraph_out[0];
+    cudaStream_t outer = c->stream, inner = nullptr;
+    st = check_cuda(c, cudaStreamCreateWithFlags(&inner, cudaStreamNonBlocking), "body stream");
+    if (st) return st;
+    st = check_cuda(c, cudaStreamBeginCaptureToGraph(inner, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed),
+                    "body capture");
+    if (!st) {
+        c->stream = inner;
+        st = body(h);
+        c->stream = outer;
+        cudaGraph_t got = nullptr;
+        les_status st2 = check_cuda(c, cudaStreamEndCapture(inner, &got), "end body capture");
+        if (!st) st = st2;
+    }
+    cudaStreamDestroy(inner);
+    if (st) return st;
+    return check_cuda(c, cudaStreamUpdateCaptureDependencies(outer, &node, nullptr, 1, cudaStreamSetCaptureDependencies),
+                      "resume capture");
+}
+
+// Emits the mixed solve of les_mixed.cu (outer FP64 defect correction, inner
+// fused FP32 PCG) into the capture in progress on c->stream.
+les_status capture_mixed_fused(les_ctx* c, const les_pcg_opts* o, ViewF A, int keep_tol)
+{
+    SolverState* out = c->state;
+    SolverState* in = c->state + 1;
+    const int inner_cap = o->inner_max_iter > 0 ? o->inner_max_iter : o->max_iter;
+    const int max_outer = o->max_outer > 0 ? o->max_outer : 50;
+    FusedPlan P;
+    les_status st = fused_plan(c, o, A, in, out, P);
+    if (st) return st;
+    if ((st = emit_outer_start(c, o, keep_tol))) return st;   // tol, r = b - A x, ||r||
+    auto set_outer = [&](cudaGraphConditionalHandle h) -> les_status {
+        launch(c, k_cond_outer, 1, 1, (const SolverState*)out, h, max_outer, o->max_iter);
+        return check_launch(c, "outer condition");
+    };
+    auto set_inner = [&](cudaGraphConditionalHandle h) -> les_status {
+        launch(c, k_cond_inner, 1, 1, (const SolverState*)in, h, inner_cap);
+        return check_launch(c, "inner condition");
+    };
+    return capture_while(c, set_outer, [&](cudaGraphConditionalHandle ho) -> les_status {
+        les_status s2;
+        if ((s2 = emit_inner_start(c, o, inner_cap))) return s2;     // inner state from the outer residual
+        if ((s2 = emit_pass_b(c, P, true, 0, 0))) return s2;          // z = M^-1 r, rho, e = 0
+        if ((s2 = emit_pass_a(c, P, true, 0))) return s2;             // iteration 1: p1 = z
+        if ((s2 = emit_pass_b(c, P, false, 1, 1))) return s2;         //   r1 -> r0
+        s2 = capture_while(c, set_inner, [&](cudaGraphConditionalHandle hi) -> les_status {
+            les_status s3;
+            if ((s3 = emit_pass_a(c, P, false, 1))) return s3;        // p1 -> p0
+            if ((s3 = emit_pass_b(c, P, false, 0, 0))) return s3;     // r0 -> r1
+            if ((s3 = emit_pass_a(c, P, false, 0))) return s3;        // p0 -> p1
+            if ((s3 = emit_pass_b(c, P, false, 1, 1))) return s3;     // r1 -> r0
+            return set_inner(hi);
+        });
+        if (s2) return s2;
+        if ((s2 = emit_outer_update(c, P.col))) return s2;                   // x += e, r = b - A x, ||r||
+        return set_outer(ho);
+    });
 }
 
 }  // namespace les

@@ -262,11 +262,15 @@ struct les_ctx {
     int n_solid = 0;
     // matrix
     int stencil_mode = 0;         // 0 none, 1 coded, 2 stored
+    bool code_plain = false;      // coded matrix built from a solid-free mask: every code is a
+                                  // function of the cell's position
     uint8_t* code = nullptr;
     double* A[7] = {};
     bool A_valid = false;         // A[] holds the current matrix (stored, or expanded codes)
     int fused = 1;                // LES_OPT_FUSED: fused FP32 inner passes
     int opt_tma = 0;              // LES_OPT_TMA: TMA-staged fused passes where the grid allows
+    int tune_cia = 0, tune_cib = 0, tune_s = -1;   // autotuned march chunk lengths (0: occupancy rule)
+    int tune_tja = 0, tune_tjb = 0;                // autotuned strip rows of the column passes (0: default)
     struct les::TmaCache* tma = nullptr;
     les::StencilCoef coef{};
     double* L[7] = {};

@@ -77,7 +77,7 @@ __global__ void k_outer_resid(Geo g, StencilView A, const double* __restrict__ x
             double e = sqrt(rr[0]);
             st->err = e;
             st->rr = rr[0];
-            st->k = outer;
+            st->k = outer >= 0 ? outer : st->k + 1;   // outer < 0: count on the device (graph replay)
             if (e < st->tol) { st->done = 1; st->status = LES_OK; }
             else if (!isfinite(e)) { st->done = 1; st->status = LES_NONFINITE; }
         }
@@ -446,7 +446,12 @@ les_status pcg_mixed_impl(les_ctx* c, const les_pcg_opts* o, les_pcg_result* res
             batch = batch < 32 ? batch * 2 : 32;
         }
         // ---- correction and the new FP64 residual
-        launch(c, k_x_add, gr, bl, g, x, e);
+        if (c->fused && col_supported(c, o)) {
+            st = col_x_update(c);   // x += e + alpha p: the column passes defer the last update of e
+            if (st) return st;
+        } else {
+            launch(c, k_x_add, gr, bl, g, x, e);
+        }
         ++outer;
         launch_p(c, PROF_OUTER, k_outer_resid, gr, bl, g, A, x, b, r, c->partials, c->counters + 8, out, outer);
         st = check_launch(c, "outer correction");
@@ -463,6 +468,39 @@ les_status pcg_mixed_impl(les_ctx* c, const les_pcg_opts* o, les_pcg_result* res
     }
     if (h.done) return (les_status)h.status;
     return LES_NOT_CONVERGED;
+}
+
+ViewF view32_of(les_ctx* c) { return view32(c); }
+
+// Launch helpers for the graph-captured mixed solve (les_fused.cu): the same
+// kernels as pcg_mixed_impl, with the outer count kept on the device.
+les_status emit_outer_start(les_ctx* c, const les_pcg_opts* o, int keep_tol)
+{
+    const Geo& g = c->g;
+    launch(c, k_set_outer, 1, 1, c->state, o->tol, keep_tol);
+    launch_p(c, PROF_OUTER, k_outer_resid, cell_grid(g), cell_block(), g, stencil_view(c), (const double*)c->slot[LES_P],
+             (const double*)c->slot[LES_B], c->f[0], c->partials, c->counters + 8, c->state, 0);
+    return check_launch(c, "outer start");
+}
+
+les_status emit_inner_start(les_ctx* c, const les_pcg_opts* o, int inner_cap)
+{
+    launch(c, k_inner_init, 1, 1, c->state + 1, (const SolverState*)c->state, o->inner_rtol, inner_cap);
+    return check_launch(c, "inner start");
+}
+
+les_status emit_outer_update(les_ctx* c, bool deferred)
+{
+    const Geo& g = c->g;
+    if (deferred) {
+        les_status st = col_x_update(c);
+        if (st) return st;
+    } else {
+        launch(c, k_x_add, cell_grid(g), cell_block(), g, c->slot[LES_P], (const float*)c->f[5]);
+    }
+    launch_p(c, PROF_OUTER, k_outer_resid, cell_grid(g), cell_block(), g, stencil_view(c), (const double*)c->slot[LES_P],
+             (const double*)c->slot[LES_B], c->f[0], c->partials, c->counters + 8, c->state, -1);
+    return check_launch(c, "outer update");
 }
 
 les_status pcg_mixed(les_ctx* c, const les_pcg_opts* o, les_pcg_result* res)

@@ -28,26 +28,29 @@ struct ViewF {
         a.c = k.c0; a.w = a.e = k.x1; a.s = a.n = k.y1; a.b = a.t = k.z1;
         return a;
     }
-    __device__ __forceinline__ CoefF at(int id) const
+    // coefficients of stencil code cd (device-built matrix)
+    __device__ __forceinline__ CoefF from_code(unsigned cd) const
     {
         CoefF a;
-        if (code) {
-            unsigned cd = code[id];
-            if (cd == 1u) return base();
-            if (cd == 0u) {
-                a.c = 1.f; a.w = a.e = a.s = a.n = a.b = a.t = 0.f;
-                return a;
-            }
-            unsigned c = cd - 1u, xs = c % 5u, r = c / 5u, ys = r & 3u, zs = r >> 2;
-            a.c = k.c0;
-            a.w = self((XW_PACK >> (2 * xs)) & 3u, k.x1, k.x2);
-            a.e = self((XE_PACK >> (2 * xs)) & 3u, k.x1, k.x2);
-            a.s = self((YL_PACK >> (2 * ys)) & 3u, k.y1, k.y2);
-            a.n = self((YH_PACK >> (2 * ys)) & 3u, k.y1, k.y2);
-            a.b = self((YL_PACK >> (2 * zs)) & 3u, k.z1, k.z2);
-            a.t = self((YH_PACK >> (2 * zs)) & 3u, k.z1, k.z2);
+        if (cd == 1u) return base();
+        if (cd == 0u) {
+            a.c = 1.f; a.w = a.e = a.s = a.n = a.b = a.t = 0.f;
             return a;
         }
+        unsigned c = cd - 1u, xs = c % 5u, r = c / 5u, ys = r & 3u, zs = r >> 2;
+        a.c = k.c0;
+        a.w = self((XW_PACK >> (2 * xs)) & 3u, k.x1, k.x2);
+        a.e = self((XE_PACK >> (2 * xs)) & 3u, k.x1, k.x2);
+        a.s = self((YL_PACK >> (2 * ys)) & 3u, k.y1, k.y2);
+        a.n = self((YH_PACK >> (2 * ys)) & 3u, k.y1, k.y2);
+        a.b = self((YL_PACK >> (2 * zs)) & 3u, k.z1, k.z2);
+        a.t = self((YH_PACK >> (2 * zs)) & 3u, k.z1, k.z2);
+        return a;
+    }
+    __device__ __forceinline__ CoefF at(int id) const
+    {
+        if (code) return from_code(code[id]);
+        CoefF a;
         a.c = d[0][id]; a.n = d[1][id]; a.s = d[2][id]; a.e = d[3][id];
         a.w = d[4][id]; a.t = d[5][id]; a.b = d[6][id];
         return a;
@@ -59,8 +62,81 @@ struct ViewF {
     }
 };
 
+// Chebyshev recurrence coefficients in FP32 (les-model src/pressure.cpp:871-905):
+// z_0 = a0 r; level k: pc_k = b[k-1] pc_{k-1} + (r - A z_{k-1}), z_k = z_{k-1} + a[k-1] pc_k.
+struct ChebF {
+    float a0;
+    float a[8], b[8];
+};
+
+// Inner products of the fused passes: per-thread double-float (TwoSum /
+// TwoProd, ~48-bit significand) accumulation, summed across threads and
+// blocks in FP64.  GB300's FP64 pipe is ~70x slower than its FP32 pipe.
+struct Acc {
+    float hi = 0.f, lo = 0.f;
+};
+
+__device__ __forceinline__ void acc_add(Acc& a, float x)
+{
+    float s = __fadd_rn(a.hi, x);
+    float bp = __fsub_rn(s, a.hi);
+    float err = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bp)), __fsub_rn(x, bp));
+    a.hi = s;
+    a.lo = __fadd_rn(a.lo, err);
+}
+
+__device__ __forceinline__ void acc_prod(Acc& a, float x, float y)
+{
+    float p = __fmul_rn(x, y);
+    float pe = __fmaf_rn(x, y, -p);   // exact low part of x*y
+    acc_add(a, p);
+    a.lo = __fadd_rn(a.lo, pe);
+}
+
+__device__ __forceinline__ double acc_value(const Acc& a) { return (double)a.hi + (double)a.lo; }
+
+ChebF cheb_coefs(const les_pcg_opts* o);
 bool fused_supported(const les_pcg_opts* o);
+
+// ---- register-column passes (les_col.cu) ----------------------------------
+// Work split of one pass: warp `item` owns k-strip item % tiles_k, row strip
+// (item / tiles_k) % tiles_j and plane chunk item / (tiles_k * tiles_j).
+struct ColMap {
+    int tk;        // output cells of a strip along k (32 minus twice the halo)
+    int tj;        // output rows of a strip along j
+    int tiles_k, tiles_j;
+    int ci;        // planes per chunk
+    int items;     // strips x chunks = warps with work
+};
+
+struct ColPlan {
+    int S = 0;             // Chebyshev levels (degree - 1); 0 = Jacobi
+    ChebF cf{};
+    float inv_c0 = 1.f;
+    ColMap ma{}, mb{};
+    int blocks_a = 0, blocks_b = 0;
+    ViewF A{};
+    SolverState* in = nullptr;
+    SolverState* out = nullptr;
+    int cap = 0;
+};
+
+// the column passes serve this solve (device-built matrix, Jacobi or
+// Chebyshev degree 2..7, option LES_OPT_FUSED = 1 without TMA)
+bool col_supported(const les_ctx* c, const les_pcg_opts* o);
+les_status col_plan(les_ctx* c, const les_pcg_opts* o, ViewF A, SolverState* in, SolverState* out, ColPlan& P);
+// pass A: p_new = pb[pc ^ 1] from z and p_old = pb[pc]; pass B: r[rin] -> r[rin ^ 1]
+les_status col_pass_a(les_ctx* c, const ColPlan& P, bool first, int pc);
+les_status col_pass_b(les_ctx* c, const ColPlan& P, bool first, int rin);
+// x += e + alpha p_last: the update the column passes defer to the end of the solve
+les_status col_x_update(les_ctx* c);
 les_status inner_solve_fused(les_ctx* c, const les_pcg_opts* o, ViewF A, SolverState* in, SolverState* out,
                              int inner_cap);
+// graph capture of the whole mixed solve (fused inner iteration)
+les_status emit_outer_start(les_ctx* c, const les_pcg_opts* o, int keep_tol);
+les_status emit_inner_start(les_ctx* c, const les_pcg_opts* o, int inner_cap);
+les_status emit_outer_update(les_ctx* c, bool deferred);
+les_status capture_mixed_fused(les_ctx* c, const les_pcg_opts* o, ViewF A, int keep_tol);
+ViewF view32_of(les_ctx* c);
 
 }  // namespace les

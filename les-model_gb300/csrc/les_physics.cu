@@ -167,13 +167,16 @@ __global__ void k_velocity_faces(Geo g, const uint8_t* __restrict__ solid, doubl
 
 // solve_momentum, src/main.cpp:563-654 (interior; the swap of :656-658 is a
 // pointer swap on the host).  One thread updates all three components.
+// dtp != nullptr: dt is read from device memory (a graph-captured step whose
+// dt comes from compute_adaptive_dt on the device).
 __global__ void k_momentum(Geo g, StepConst s, double dt, double nu, const double* __restrict__ u,
                            const double* __restrict__ v, const double* __restrict__ w,
                            const double* __restrict__ nu_t, double* __restrict__ un,
-                           double* __restrict__ vn, double* __restrict__ wn)
+                           double* __restrict__ vn, double* __restrict__ wn, const double* dtp)
 {
     int i, j, k;
     if (!cell_coords(g, i, j, k)) return;
+    if (dtp) dt = *dtp;
     if (i < 1 || i > g.nx - 2 || j < 1 || j > g.ny - 2 || k < 1 || k > g.nz - 2) return;
     const int id = i * g.si + j * g.sj + k, si = g.si, sj = g.sj;
     const double nu_eff = nu + nu_t[id];
@@ -197,10 +200,12 @@ __global__ void k_momentum(Geo g, StepConst s, double dt, double nu, const doubl
 
 // correct_velocity, src/main.cpp:671-714 (interior).
 __global__ void k_correct(Geo g, StepConst s, double dt_over_rho, const double* __restrict__ p,
-                          double* __restrict__ u, double* __restrict__ v, double* __restrict__ w)
+                          double* __restrict__ u, double* __restrict__ v, double* __restrict__ w,
+                          const double* dtp, double rho)
 {
     int i, j, k;
     if (!cell_coords(g, i, j, k)) return;
+    if (dtp) dt_over_rho = *dtp / rho;   // src/main.cpp:677, from the device dt
     if (i < 1 || i > g.nx - 2 || j < 1 || j > g.ny - 2 || k < 1 || k > g.nz - 2) return;
     const int id = i * g.si + j * g.sj + k;
     u[id] -= dt_over_rho * ((p[id + g.si] - p[id - g.si]) * s.inv_2dx);
@@ -306,24 +311,24 @@ les_status sgs_nut_dev(les_ctx* c, double cs, int want_tau)
     return check_launch(c, "sgs+nut");
 }
 
-les_status momentum_dev(les_ctx* c, double dt, double nu)
+les_status momentum_dev(les_ctx* c, double dt, double nu, const double* dtp)
 {
     const Geo& g = c->g;
-    launch(c, k_momentum, cell_grid(g), cell_block(), 
+    launch(c, k_momentum, cell_grid(g), cell_block(),
         g, step_const(c->mesh), dt, nu, c->slot[LES_U], c->slot[LES_V], c->slot[LES_W],
-        c->slot[LES_NU_T], c->slot[LES_U_NEW], c->slot[LES_V_NEW], c->slot[LES_W_NEW]);
+        c->slot[LES_NU_T], c->slot[LES_U_NEW], c->slot[LES_V_NEW], c->slot[LES_W_NEW], dtp);
     std::swap(c->slot[LES_U], c->slot[LES_U_NEW]);
     std::swap(c->slot[LES_V], c->slot[LES_V_NEW]);
     std::swap(c->slot[LES_W], c->slot[LES_W_NEW]);
     return check_launch(c, "momentum");
 }
 
-les_status correct_dev(les_ctx* c, double dt, double rho)
+les_status correct_dev(les_ctx* c, double dt, double rho, const double* dtp)
 {
     const Geo& g = c->g;
     launch(c, k_correct, cell_grid(g), cell_block(), g, step_const(c->mesh), dt / rho,
                                                              c->slot[LES_P], c->slot[LES_U],
-                                                             c->slot[LES_V], c->slot[LES_W]);
+                                                             c->slot[LES_V], c->slot[LES_W], dtp, rho);
     return check_launch(c, "correct velocity");
 }
 
@@ -404,14 +409,14 @@ les_status les_momentum(les_ctx* c, double dt, double nu)
 {
     if (!c) return LES_BAD_ARG;
     cudaSetDevice(c->device);
-    return momentum_dev(c, dt, nu);
+    return momentum_dev(c, dt, nu, nullptr);
 }
 
 les_status les_correct_velocity(les_ctx* c, double dt, double rho)
 {
     if (!c) return LES_BAD_ARG;
     cudaSetDevice(c->device);
-    return correct_dev(c, dt, rho);
+    return correct_dev(c, dt, rho, nullptr);
 }
 
 }  // extern "C"

@@ -58,11 +58,12 @@ __global__ void k_div_b(Geo g, double scale, double idx, double idy, double idz,
                         const double* __restrict__ vn, const double* __restrict__ wn,
                         const uint8_t* __restrict__ solid, double* __restrict__ rhs,
                         double* __restrict__ b, double* partials, unsigned* counter, SolverState* st,
-                        double rel_tol)
+                        double rel_tol, const double* dtp, double rho)
 {
     __shared__ double sm[32];
     int i, j, k;
     double bb[1] = {0.0};
+    if (dtp) scale = rho / *dtp;   // src/pressure.cpp:260, from the device dt
     if (cell_coords(g, i, j, k)) {
         const int id = i * g.si + j * g.sj + k;
         double r = 0.0;
@@ -105,11 +106,13 @@ __global__ void k_build_b(Geo g, const double* __restrict__ rhs, const uint8_t* 
 }
 
 // build_stencil (src/pressure.cpp:608-699) as one code byte per cell.
-__global__ void k_build_code(Geo g, const uint8_t* __restrict__ solid, uint8_t* __restrict__ code)
+__global__ void k_build_code(Geo g, const uint8_t* __restrict__ solid, uint8_t* __restrict__ code,
+                             unsigned* any_solid)
 {
     int i, j, k;
     if (!cell_coords(g, i, j, k)) return;
     const int id = i * g.si + j * g.sj + k;
+    if (solid[id]) *any_solid = 1u;   // every writer stores the same value
     if (solid[id] || i == g.nx - 1) { code[id] = 0; return; }
     bool W = (i == 0) || solid[id - g.si];
     bool E1 = (i == g.nx - 2);
@@ -510,13 +513,13 @@ les_status dot_dev(les_ctx* c, const double* a, const double* b, double* out_hos
     return LES_OK;
 }
 
-les_status div_b_dev(les_ctx* c, double dt, double rho, double rel_tol)
+les_status div_b_dev(les_ctx* c, double dt, double rho, double rel_tol, const double* dtp)
 {
     const les_mesh& m = c->mesh;
-    launch(c, k_div_b, cell_grid(c->g), cell_block(), 
+    launch(c, k_div_b, cell_grid(c->g), cell_block(),
         c->g, rho / dt, 1.0 / (2.0 * m.dx), 1.0 / (2.0 * m.dy), 1.0 / (2.0 * m.dz), 1.0 / m.dx,
         1.0 / m.dy, 1.0 / m.dz, c->slot[LES_U_NEW], c->slot[LES_V_NEW], c->slot[LES_W_NEW], c->mask,
-        c->slot[LES_P_RHS], c->slot[LES_B], c->partials, c->counters + 3, c->state, rel_tol);
+        c->slot[LES_P_RHS], c->slot[LES_B], c->partials, c->counters + 3, c->state, rel_tol, dtp, rho);
     return check_launch(c, "divergence+b");
 }
 
@@ -716,7 +719,7 @@ les_status les_divergence(les_ctx* c, double dt, double rho)
     launch(c, k_div_b, cell_grid(c->g), cell_block(), 
         c->g, rho / dt, 1.0 / (2.0 * m.dx), 1.0 / (2.0 * m.dy), 1.0 / (2.0 * m.dz), 1.0 / m.dx,
         1.0 / m.dy, 1.0 / m.dz, c->slot[LES_U_NEW], c->slot[LES_V_NEW], c->slot[LES_W_NEW], c->mask,
-        c->slot[LES_P_RHS], nullptr, c->partials, c->counters + 3, c->state, 0.0);
+        c->slot[LES_P_RHS], nullptr, c->partials, c->counters + 3, c->state, 0.0, nullptr, rho);
     return check_launch(c, "divergence");
 }
 
@@ -751,10 +754,18 @@ les_status les_build_stencil(les_ctx* c)
     c->coef.x1 = -idx2; c->coef.x2 = -idx2 + -idx2;
     c->coef.y1 = -idy2; c->coef.y2 = -idy2 + -idy2;
     c->coef.z1 = -idz2; c->coef.z2 = -idz2 + -idz2;
-    launch(c, k_build_code, cell_grid(c->g), cell_block(), c->g, c->mask, c->code);
+    unsigned* any_solid = c->counters + 30;
+    les_status st = check_cuda(c, cudaMemsetAsync(any_solid, 0, sizeof(unsigned), c->stream), "memset");
+    if (st) return st;
+    launch(c, k_build_code, cell_grid(c->g), cell_block(), c->g, c->mask, c->code, any_solid);
     c->stencil_mode = 1;
     c->A_valid = false;   // a stale expansion of an older matrix must not be used
-    return check_launch(c, "build stencil");
+    if ((st = check_launch(c, "build stencil"))) return st;
+    unsigned h = 1;
+    st = check_cuda(c, cudaMemcpyAsync(&h, any_solid, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream), "copy");
+    if (!st) st = check_cuda(c, cudaStreamSynchronize(c->stream), "build stencil");
+    c->code_plain = st == LES_OK && h == 0u;
+    return st;
 }
 
 les_status les_get_stencil(les_ctx* c, double* const* diag7)

@@ -11,10 +11,10 @@ using namespace les;
 namespace les {
 les_status velocity_bcs_dev(les_ctx* c);
 les_status sgs_nut_dev(les_ctx* c, double cs, int want_tau);
-les_status momentum_dev(les_ctx* c, double dt, double nu);
-les_status correct_dev(les_ctx* c, double dt, double rho);
+les_status momentum_dev(les_ctx* c, double dt, double nu, const double* dtp);
+les_status correct_dev(les_ctx* c, double dt, double rho, const double* dtp);
 les_status adaptive_dt_dev(les_ctx* c, double nu, double cfl_conv, double cfl_visc, double dt_max);
-les_status div_b_dev(les_ctx* c, double dt, double rho, double rel_tol);
+les_status div_b_dev(les_ctx* c, double dt, double rho, double rel_tol, const double* dtp);
 les_status pcg_fp64(les_ctx* c, const les_pcg_opts* o, les_pcg_result* res, int keep_tol);
 les_status pcg_mixed_impl(les_ctx* c, const les_pcg_opts* o, les_pcg_result* res, int keep_tol);
 les_status solve_jacobi_dev(les_ctx* c, double dt, double rho, int max_iter, double tol, int* sweeps);
@@ -38,13 +38,13 @@ extern "C" les_status les_step(les_ctx* c, const les_step_params* prm, les_step_
         dt = c->h_state[0].scal[0];
     }
     if ((st = sgs_nut_dev(c, prm->cs, prm->want_tau))) return st;
-    if ((st = momentum_dev(c, dt, prm->nu))) return st;
+    if ((st = momentum_dev(c, dt, prm->nu, nullptr))) return st;
     if ((st = velocity_bcs_dev(c))) return st;
     les_status solve = LES_OK;
     les_step_stats s{};
     s.dt = dt;
     if (prm->solver == LES_SOLVER_PCG) {
-        if ((st = div_b_dev(c, dt, prm->rho, prm->rel_tol))) return st;
+        if ((st = div_b_dev(c, dt, prm->rho, prm->rel_tol, nullptr))) return st;
         les_pcg_result r{};
         const int keep = prm->rel_tol > 0 ? 1 : 0;
         if (prm->pcg.precision == LES_MIXED) solve = pcg_mixed_impl(c, &prm->pcg, &r, keep);
@@ -61,7 +61,7 @@ extern "C" les_status les_step(les_ctx* c, const les_step_params* prm, les_step_
         solve = solve_gs_dev(c, dt, prm->rho, prm->stat_max_iter, prm->omega, prm->stat_tol, &s.iters);
         if (solve != LES_OK) return solve;
     }
-    if ((st = correct_dev(c, dt, prm->rho))) return st;
+    if ((st = correct_dev(c, dt, prm->rho, nullptr))) return st;
     if ((st = velocity_bcs_dev(c))) return st;
     s.status = solve;
     if (stats) *stats = s;

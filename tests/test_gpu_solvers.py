@@ -189,31 +189,33 @@ def _odd_system(shape, seed):
     return m, b, lmax
 
 
-@pytest.mark.parametrize("shape", [(45, 37, 70), (70, 19, 33)], ids=["45x37x70", "70x19x33"])
+@pytest.mark.parametrize("shape", [(45, 37, 70), (70, 19, 33), (12, 7, 29)], ids=["45x37x70", "70x19x33", "12x7x29"])
 @pytest.mark.parametrize("pc,deg", [(G.PC_CHEBYSHEV, 3), (G.PC_CHEBYSHEV, 4), (G.PC_CHEBYSHEV, 5),
-                                    (G.PC_JACOBI, 0)], ids=["cheb3", "cheb4", "cheb5", "jacobi"])
-def test_fused_inner_matches_unfused(shape, pc, deg):
-    """The fused two-pass FP32 inner iteration (temporally blocked Chebyshev)
-    follows the same iteration as the one-kernel-per-operation path: same
-    converged solution (pressure within the mixed-vs-FP64 bar, 1e-6
-    relative) with inner iteration counts within 15% (FP32 CG on this
-    non-symmetric system is sensitive to rounding: the two paths round their
-    inner products differently)."""
+                                    (G.PC_CHEBYSHEV, 7), (G.PC_JACOBI, 0)],
+                         ids=["cheb3", "cheb4", "cheb5", "cheb7", "jacobi"])
+@pytest.mark.parametrize("fused", [1, 2], ids=["columns", "tiles"])
+def test_fused_inner_matches_unfused(shape, pc, deg, fused):
+    """The fused two-pass FP32 inner iterations (register-column marches and
+    shared-memory tiles, both with temporally blocked Chebyshev levels) follow
+    the same iteration as the one-kernel-per-operation path: same converged
+    solution (pressure within the mixed-vs-FP64 bar, 1e-6 relative) with
+    inner iteration counts within 15% (FP32 CG on this non-symmetric system is
+    sensitive to rounding: the paths round their inner products differently)."""
     m, b, lmax = _odd_system(shape, sum(shape) + deg)
     tol = 1e-8 * np.linalg.norm(b)
     res = {}
-    for fused in (1, 0):
+    for mode in (fused, 0):
         with G.Context(m) as c:
-            c.set_option(G.OPT_FUSED, fused)
+            c.set_option(G.OPT_FUSED, mode)
             c.upload_mask(np.zeros(m.n, np.uint8))
             c.build_stencil()
             c.upload("b", b)
             c.upload("p", np.zeros(m.n))
             st, r = c.pcg(G.pcg_opts(precond=pc, max_iter=20000, tol=tol, lambda_min=3 * np.pi ** 2,
                                      lambda_max=lmax, degree=max(deg, 1), precision=G.MIXED, inner_rtol=1e-4))
-            res[fused] = (st, r.iters, r.outer, r.residual, c.download("p"))
-    (s1, i1, o1, r1, x1), (s0, i0, o0, r0, x0) = res[1], res[0]
-    assert s1 == G.OK and s0 == G.OK, (res[1][:4], res[0][:4])
+            res[mode] = (st, r.iters, r.outer, r.residual, c.download("p"))
+    (s1, i1, o1, r1, x1), (s0, i0, o0, r0, x0) = res[fused], res[0]
+    assert s1 == G.OK and s0 == G.OK, (res[fused][:4], res[0][:4])
     assert r1 < tol and r0 < tol
     assert abs(i1 - i0) <= max(2, 0.15 * i0), (i1, i0)
     assert maxrel(x1, x0) < 1e-6, maxrel(x1, x0)
@@ -223,14 +225,14 @@ def test_fused_inner_matches_unfused(shape, pc, deg):
 @pytest.mark.parametrize("pc,deg", [(G.PC_CHEBYSHEV, 4), (G.PC_CHEBYSHEV, 6), (G.PC_JACOBI, 0)],
                          ids=["cheb4", "cheb6", "jacobi"])
 def test_tma_fused_matches_plain_fused(shape, pc, deg):
-    """With nz % 16 == 0 the fused passes stage their planes with TMA; the
-    result must match the same passes with plain loads (identical arithmetic:
+    """With nz % 16 == 0 the shared-memory tile passes stage their planes with
+    TMA; the result must match the same passes with plain loads (identical arithmetic:
     equal iteration counts, pressure equal to rounding of the final outer
     correction) and the unfused path (mixed-vs-FP64 bar)."""
     m, b, lmax = _odd_system(shape, sum(shape) + deg)
     tol = 1e-8 * np.linalg.norm(b)
     res = {}
-    for tma, fused in ((1, 1), (0, 1), (0, 0)):
+    for tma, fused in ((1, 2), (0, 2), (0, 0)):
         with G.Context(m) as c:
             c.set_option(G.OPT_FUSED, fused)
             c.set_option(G.OPT_TMA, tma)
@@ -241,7 +243,7 @@ def test_tma_fused_matches_plain_fused(shape, pc, deg):
             st, r = c.pcg(G.pcg_opts(precond=pc, max_iter=20000, tol=tol, lambda_min=3 * np.pi ** 2,
                                      lambda_max=lmax, degree=max(deg, 1), precision=G.MIXED, inner_rtol=1e-4))
             res[(tma, fused)] = (st, r.iters, r.outer, r.residual, c.download("p"))
-    t, f, u = res[(1, 1)], res[(0, 1)], res[(0, 0)]
+    t, f, u = res[(1, 2)], res[(0, 2)], res[(0, 0)]
     assert t[0] == G.OK and f[0] == G.OK and u[0] == G.OK, (t[:4], f[:4], u[:4])
     assert t[1] == f[1] and t[2] == f[2], (t[:4], f[:4])
     assert maxrel(t[4], f[4]) < 1e-12, maxrel(t[4], f[4])
