@@ -234,7 +234,11 @@ typedef enum les_option {
     LES_OPT_ROWS_B = 3,   /* rows per strip of pass B: 16 (Jacobi), 4 or 8
                              (Chebyshev degree 2..4), 4 (degree 5..7) */
     LES_OPT_CHUNK_A = 4,  /* planes per march chunk of pass A */
-    LES_OPT_CHUNK_B = 5   /* planes per march chunk of pass B */
+    LES_OPT_CHUNK_B = 5,  /* planes per march chunk of pass B */
+    LES_OPT_GRAPH = 6     /* 1 (default): les_step with the mixed-precision fused PCG
+                             runs as one CUDA graph launch (captured per velocity
+                             buffer parity, both solver loops as conditional nodes;
+                             not while les_profile records); 0: launch by launch */
 } les_option;
 les_status les_set_option(les_ctx* ctx, int option, int value);
 

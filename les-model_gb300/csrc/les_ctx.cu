@@ -194,6 +194,9 @@ void les_destroy(les_ctx* c)
     for (auto& e : c->prof_ev) cudaEventDestroy(e);
     for (auto& e : c->marks) cudaEventDestroy(e);
     les::tma_cache_free(c->tma);
+    les::step_graph_free(c->sg[0]);
+    les::step_graph_free(c->sg[1]);
+    if (c->aux) cudaStreamDestroy(c->aux);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -241,6 +244,7 @@ les_status les_upload_mask(les_ctx* c, const uint8_t* solid)
 {
     if (!c || !solid) return LES_BAD_ARG;
     cudaSetDevice(c->device);
+    ++c->version;   // the solid-cell list is baked into captured step graphs
     const Geo& g = c->g;
     std::vector<uint8_t> m01(g.n);
     std::vector<int> list;
@@ -314,6 +318,7 @@ les_status les_set_stencil(les_ctx* c, const double* const* diag7)
     les_status st = put_diag7(c, c->A, diag7);
     if (st) return st;
     c->stencil_mode = 2;
+    ++c->version;
     c->A_valid = true;
     return LES_OK;
 }
@@ -335,7 +340,9 @@ unsigned long long les_launch_count(const les_ctx* c) { return c ? c->launches :
 les_status les_set_option(les_ctx* c, int option, int value)
 {
     if (!c) return LES_BAD_ARG;
+    ++c->version;   // captured step graphs depend on every option
     switch (option) {
+    case LES_OPT_GRAPH: c->graph_on = value ? 1 : 0; return LES_OK;
     case LES_OPT_FUSED: c->fused = value == 2 ? 2 : (value ? 1 : 0); return LES_OK;
     case LES_OPT_TMA: c->opt_tma = value ? 1 : 0; return LES_OK;
     case LES_OPT_ROWS_A: c->tune_tja = value; return LES_OK;

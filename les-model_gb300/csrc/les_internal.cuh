@@ -21,6 +21,8 @@ namespace les {
 
 struct TmaCache;                       // tensor maps of the fused passes (les_fused.cu)
 void tma_cache_free(TmaCache* t);
+struct StepGraph;                      // captured time step (les_step.cu)
+void step_graph_free(StepGraph* s);
 
 // ---- geometry -------------------------------------------------------------
 struct Geo {
@@ -298,6 +300,13 @@ struct les_ctx {
     std::vector<cudaEvent_t> prof_ev;     // pool, two per recorded launch
     std::vector<int> prof_id;             // kernel id of each recorded pair
     std::vector<cudaEvent_t> marks;       // les_mark slots
+    // CUDA-graph time steps (les_step.cu): one executable graph per velocity
+    // buffer parity, rebuilt when anything baked into it changes
+    int graph_on = 1;                     // LES_OPT_GRAPH
+    cudaStream_t aux = nullptr;           // capture stream for conditional-loop bodies
+    struct les::StepGraph* sg[2] = {};
+    int sg_last = 0;                      // slot of the graph launched last
+    unsigned long long version = 0;       // bumped by every change a captured graph depends on
 };
 
 namespace les {

@@ -759,6 +759,7 @@ les_status les_build_stencil(les_ctx* c)
     if (st) return st;
     launch(c, k_build_code, cell_grid(c->g), cell_block(), c->g, c->mask, c->code, any_solid);
     c->stencil_mode = 1;
+    ++c->version;
     c->A_valid = false;   // a stale expansion of an older matrix must not be used
     if ((st = check_launch(c, "build stencil"))) return st;
     unsigned h = 1;

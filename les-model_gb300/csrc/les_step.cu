@@ -3,8 +3,11 @@
 // pressure solve, projection, velocity BCs.  Statistics and VTK output
 // (:152-164) stay with the caller.
 #include <cmath>
+#include <cstring>
+#include <utility>
 
 #include "les_internal.cuh"
+#include "les_mixed.cuh"
 
 using namespace les;
 
@@ -21,6 +24,136 @@ les_status solve_jacobi_dev(les_ctx* c, double dt, double rho, int max_iter, dou
 les_status solve_gs_dev(les_ctx* c, double dt, double rho, int max_iter, double omega, double tol, int* sweeps);
 }
 
+// ---- the time step as a CUDA graph -------------------------------------------
+// With the mixed-precision fused PCG every decision of a step can be taken on
+// the device: dt comes from the CFL reduction through a device pointer, and
+// both solver loops are conditional graph nodes (les_fused.cu).  The whole
+// step is captured once per velocity-buffer parity (the momentum update swaps
+// u and u_new, and a graph holds fixed pointers) and replayed with one launch.
+namespace les {
+
+struct StepGraph {
+    les_step_params prm{};
+    double* slots[LES_NSLOTS] = {};
+    double* tau = nullptr;
+    unsigned long long version = 0;
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long captured = 0;   // kernel nodes outside and inside one pass of each loop
+};
+
+void step_graph_free(StepGraph* s)
+{
+    if (!s) return;
+    if (s->exec) cudaGraphExecDestroy(s->exec);
+    delete s;
+}
+
+}  // namespace les
+
+static bool graph_eligible(const les_ctx* c, const les_step_params* prm)
+{
+    return c->graph_on && !c->prof_on && prm->solver == LES_SOLVER_PCG && prm->pcg.precision == LES_MIXED &&
+           c->stencil_mode == 1 && c->fused && fused_supported(&prm->pcg) && prm->pcg.max_iter > 0;
+}
+
+static bool graph_matches(const les_ctx* c, const StepGraph* s, const les_step_params* prm)
+{
+    return s && s->exec && s->version == c->version && s->tau == c->tau &&
+           std::memcmp(&s->prm, prm, sizeof *prm) == 0 && std::memcmp(s->slots, c->slot, sizeof s->slots) == 0;
+}
+
+// One step (src/main.cpp:115-144) into the capture in progress on c->stream.
+static les_status emit_step(les_ctx* c, const les_step_params* prm)
+{
+    les_status st;
+    double dt = prm->dt_fixed;
+    const double* dtp = nullptr;
+    if (!(dt > 0)) {
+        if ((st = adaptive_dt_dev(c, prm->nu, prm->cfl_conv, prm->cfl_visc, prm->dt_max))) return st;
+        dtp = &c->state[0].scal[0];   // nothing else in the step writes it
+        dt = 1.0;                     // unused: the kernels read *dtp
+    }
+    if ((st = sgs_nut_dev(c, prm->cs, prm->want_tau))) return st;
+    if ((st = momentum_dev(c, dt, prm->nu, dtp))) return st;
+    if ((st = velocity_bcs_dev(c))) return st;
+    if ((st = div_b_dev(c, dt, prm->rho, prm->rel_tol, dtp))) return st;
+    if ((st = capture_mixed_fused(c, &prm->pcg, view32_of(c), prm->rel_tol > 0 ? 1 : 0))) return st;
+    if ((st = correct_dev(c, dt, prm->rho, dtp))) return st;
+    return velocity_bcs_dev(c);
+}
+
+static les_status step_graph(les_ctx* c, const les_step_params* prm, les_step_stats* stats)
+{
+    les_status st = ensure_work(c);
+    if (!st) st = ensure_work32(c);
+    if (st) return st;
+    StepGraph* g = graph_matches(c, c->sg[0], prm) ? c->sg[0] : (graph_matches(c, c->sg[1], prm) ? c->sg[1] : nullptr);
+    bool fresh = false;
+    if (!g) {
+        // capture into an empty or stale slot, else replace the graph not used last
+        int k = -1;
+        for (int q = 0; q < 2 && k < 0; ++q)
+            if (!c->sg[q] || c->sg[q]->version != c->version || std::memcmp(&c->sg[q]->prm, prm, sizeof *prm) != 0)
+                k = q;
+        if (k < 0) k = c->sg_last ^ 1;
+        step_graph_free(c->sg[k]);
+        c->sg[k] = g = new StepGraph();
+        g->prm = *prm;
+        std::memcpy(g->slots, c->slot, sizeof g->slots);
+        g->version = c->version;
+        double* before[LES_NSLOTS];
+        std::memcpy(before, c->slot, sizeof before);
+        const unsigned long long l0 = c->launches;
+        cudaGraph_t graph = nullptr;
+        st = check_cuda(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed), "begin step capture");
+        if (st) return st;
+        les_status st1 = emit_step(c, prm);
+        les_status st2 = check_cuda(c, cudaStreamEndCapture(c->stream, &graph), "end step capture");
+        g->captured = c->launches - l0;
+        c->launches = l0;
+        g->tau = c->tau;
+        if (!st1 && !st2)
+            st1 = check_cuda(c, cudaGraphInstantiate(&g->exec, graph, 0), "instantiate step graph");
+        if (graph) cudaGraphDestroy(graph);
+        if (st1 || st2) {
+            std::memcpy(c->slot, before, sizeof before);   // nothing ran: undo the capture's buffer swap
+            step_graph_free(g);
+            c->sg[k] = nullptr;
+            return st1 ? st1 : st2;
+        }
+        fresh = true;
+    }
+    st = check_cuda(c, cudaGraphLaunch(g->exec, c->stream), "launch step graph");
+    if (st) return st;
+    c->sg_last = g == c->sg[0] ? 0 : 1;
+    if (!fresh) {   // the captured momentum update swapped the buffers on the host only once
+        std::swap(c->slot[LES_U], c->slot[LES_U_NEW]);
+        std::swap(c->slot[LES_V], c->slot[LES_V_NEW]);
+        std::swap(c->slot[LES_W], c->slot[LES_W_NEW]);
+    }
+    if (!stats) {
+        c->launches += g->captured;
+        return LES_OK;
+    }
+    if ((st = read_state(c))) return st;
+    const SolverState& o = c->h_state[0];
+    les_step_stats s{};
+    s.dt = prm->dt_fixed > 0 ? prm->dt_fixed : o.scal[0];
+    s.iters = o.iters;
+    s.outer = o.k;
+    s.residual = o.err;
+    s.b_norm = o.bnorm;
+    s.status = o.done ? (les_status)o.status : LES_NOT_CONVERGED;
+    *stats = s;
+    // kernels run: the captured nodes, less one pass of each loop body (13
+    // nodes), plus 8 per outer correction and 5 per pass of the two-iteration
+    // inner body
+    const long long body = (o.iters - o.k + 1) / 2;
+    const long long run = (long long)g->captured - 13 + 8LL * o.k + 5LL * (body > 0 ? body : 0);
+    c->launches += run > 0 ? (unsigned long long)run : g->captured;
+    return LES_OK;
+}
+
 extern "C" les_status les_step(les_ctx* c, const les_step_params* prm, les_step_stats* stats)
 {
     if (!c || !prm) return LES_BAD_ARG;
@@ -28,6 +161,7 @@ extern "C" les_status les_step(les_ctx* c, const les_step_params* prm, les_step_
     if (prm->solver == LES_SOLVER_PCG && !c->stencil_mode)
         return fail(c, LES_BAD_ARG, "PCG needs a matrix: call les_build_stencil first");
     cudaSetDevice(c->device);
+    if (graph_eligible(c, prm)) return step_graph(c, prm, stats);
     les_status st;
     double dt = prm->dt_fixed;
     if (!(dt > 0)) {
