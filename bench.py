@@ -55,7 +55,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
-    ap.add_argument("--workload", default="large", choices=("small", "large", "xlarge"))
+    ap.add_argument("--workload", default="large", choices=("small", "large", "xlarge", "batch"))
+    ap.add_argument("--batch", type=int, default=64, help="cases of the batch workload")
+    ap.add_argument("--tune", type=int, default=1, help="batch workload: run the ensemble autotuner first")
     ap.add_argument("--precond", default="cheb", choices=("cheb", "jacobi", "ic"))
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
@@ -133,12 +135,13 @@ class Clocks:
 # algorithmic HBM bytes per cell of one launch of each profiled kernel
 def alg_bytes_per_cell(name, fused=1):
     # fused FP32 inner passes.  Register columns (fused=1, the default): pass B
-    # reads r, q and the stencil code and writes r', z (the whole Chebyshev
-    # apply stays on chip); pass A reads z, p_old, e and the code and writes
-    # p, q, e.  Shared-memory tiles (fused=2): pass B also reads p, e and
-    # writes e; pass A reads z, p_old, code and writes p, q.
+    # reads r, q and writes r', z (the whole Chebyshev apply stays on chip);
+    # pass A reads z, p_old, e and writes p, q, e.  Shared-memory tiles
+    # (fused=2): pass B reads r, q, p, e and the stencil code and writes r',
+    # e', z; pass A reads z, p_old, code and writes p, q.
     if fused == 1 and name in ("inner_precond_f32", "inner_spmv_f32"):
-        return {"inner_precond_f32": 17.0, "inner_spmv_f32": 25.0}[name]
+        # the column passes take the matrix from the cell position (no code byte)
+        return {"inner_precond_f32": 16.0, "inner_spmv_f32": 24.0}[name]
     return {"inner_precond_f32": 29.0, "inner_spmv_f32": 17.0, "inner_update_f32": 28.0, "spmv_f64": 17.0,
             "update_f64": 48.0, "cheb_f64": 41.0, "outer_resid_f64": 21.0}.get(name)
 
@@ -227,6 +230,10 @@ def run_reference(args):
     if rank != 0:
         return 0
     import les_cases
+    if args.workload not in REF_ITERS:
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU arm times single cases "
+                          "(small, large, xlarge); the ensemble workload has no CPU counterpart"}), flush=True)
+        return 0
     shape, h, solid, f = les_cases.case(args.workload, args.seed)
     n = int(np.prod(shape))
     iters = REF_ITERS[args.workload]
@@ -249,6 +256,81 @@ def run_reference(args):
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_batch(args):
+    """Ensemble workload: `--batch` ragged cases (dims from {32..96}, random
+    cube obstacle, Cs from [0.1, 0.2], inflow noise 0.02), mixed-precision
+    Chebyshev(4)-PCG, every step one CUDA graph launch for all cases; strip
+    shapes and chunk lengths from the ensemble autotuner."""
+    import torch
+    import les_cases
+    import les_gb300 as G
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(0)
+    specs = les_cases.batch_cases(args.batch, args.seed)
+    meshes = [G.Mesh(*s["shape"], s["h"], s["h"], s["h"]) for s in specs]
+    ens = G.Ensemble(meshes)
+    prm = []
+    for c, s in zip(ens.cases, specs):
+        shape = s["shape"]
+        n = int(np.prod(shape))
+        c.upload_mask(np.zeros(n, np.uint8))
+        c.build_stencil()
+        lmax = c.lambda_max(20)
+        solid = les_cases.box_mask(shape, s["box"])
+        f = les_cases.init_fields(shape, s["noise"], s["seed"])
+        les_cases.velocity_bcs_np(shape, f, solid)
+        c.upload_fields(f)
+        c.upload_mask(solid)
+        prm.append(G.step_params(nu=les_cases.NU, rho=les_cases.RHO, cs=s["cs"], cfl_conv=les_cases.CFL_CONV,
+                                 solver=G.SOLVER_PCG, rel_tol=1e-8,
+                                 pcg=G.pcg_opts(precond=G.PC_CHEBYSHEV, max_iter=5000, lambda_min=3 * np.pi ** 2,
+                                                lambda_max=lmax, degree=4, precision=G.MIXED,
+                                                inner_rtol=args.inner_rtol)))
+    cells = sum(int(np.prod(s["shape"])) for s in specs)
+    t0 = time.perf_counter()
+    tune_us = ens.autotune(prm[0].pcg) if args.tune else None
+    tune_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for _ in range(args.warmup):
+        ens.step(prm)
+    ens.sync()
+    warm_s = time.perf_counter() - t0
+    launches0 = sum(c.launch_count() for c in ens.cases)
+    clocks = Clocks(0)
+    clocks.start()
+    iters, worst = [], 0.0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        st = ens.step(prm)
+        iters.append(statistics.mean(x.iters for x in st))
+        worst = max(worst, max(x.residual / x.b_norm for x in st if x.b_norm > 0))
+        bad = [x.status for x in st if x.status != G.OK]
+        if bad:
+            raise RuntimeError("ensemble step: %d cases did not converge" % len(bad))
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    launches = sum(c.launch_count() for c in ens.cases) - launches0
+    value = cells * args.steps / wall / 1e6
+    line = {"metric": "Mcell-steps/s, ensemble of %d ragged cases, mixed FP32/FP64 at div<=1e-8" % args.batch,
+            "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 inner / f64 outer", "data": "synthetic",
+            "config": {"workload": "batch: %d cases, dims from {32,48,64,80,96}, cube obstacle, Cs U[0.1,0.2], "
+                                   "cheb(4)-PCG mixed, one graph launch per step" % args.batch,
+                       "cells": cells, "timing": "host wall clock around each step's launch + stats sync",
+                       "l2": "inputs (~%.1f GB) larger than L2" % (cells * 120 / 1e9),
+                       "autotune_us_per_iteration": tune_us, "autotune_s": tune_s,
+                       "first_steps_with_capture_s": warm_s},
+            "gpu_launches": launches, "iters_inner_mean": statistics.mean(iters), "rel_residual_max": worst,
+            "clocks": clk}
+    print(json.dumps(line), flush=True)
+    ens.close()
     return 0
 
 
@@ -433,6 +515,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batch":
+        return run_batch(args)
     return run_ours(args)
 
 

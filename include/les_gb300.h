@@ -219,6 +219,38 @@ les_status les_axpby(les_ctx* ctx, int out_slot, double a, int in1_slot, double 
 #define LES_NOALLOC_MAX_CELLS 134217728LL
 les_status les_dot_noalloc(const double* a, const double* b, long long n, double* out, void* stream);
 
+/* ---- batched ensemble (no reference counterpart) ------------------------ */
+/* Many independent cases (each its own mesh, fields, matrix and solver
+ * state) advanced together: one CUDA graph launch per time step runs every
+ * case's whole step as an independent branch.  Set each case up through its
+ * context (les_ensemble_case: upload fields and mask, build the matrix, ...);
+ * the contexts belong to the ensemble. */
+typedef struct les_ensemble les_ensemble;
+les_status les_ensemble_create(const les_mesh* meshes, int count, int device, les_ensemble** out);
+void les_ensemble_destroy(les_ensemble* ens);
+int les_ensemble_size(const les_ensemble* ens);
+les_ctx* les_ensemble_case(les_ensemble* ens, int i);
+const char* les_ensemble_last_error(const les_ensemble* ens);
+/* One time step of every case: prm[i] for case i (each must be the
+ * mixed-precision fused PCG, Jacobi or Chebyshev, on a device-built
+ * matrix).  stats (count entries, or NULL for no host sync) as les_step. */
+les_status les_ensemble_step(les_ensemble* ens, const les_step_params* prm, les_step_stats* stats);
+les_status les_ensemble_sync(les_ensemble* ens);
+
+/* ---- autotuner (no reference counterpart) ------------------------------- */
+/* Times the fused inner passes of the mixed-precision PCG for opts on the
+ * context's current matrix over candidate strip shapes and march chunk
+ * lengths (LES_OPT_ROWS_A/B, LES_OPT_CHUNK_A/B), with `share` the fraction
+ * of the GPU the context gets while it runs (1 alone, 1/k beside k-1 other
+ * cases), and sets the fastest.  best_us (optional) receives the time of one
+ * inner iteration with the chosen shape.  The solver's work vectors are
+ * overwritten; fields and matrix are not touched. */
+les_status les_autotune(les_ctx* ctx, const les_pcg_opts* opts, double share, double* best_us);
+/* The same over all cases of an ensemble at once (every case runs its
+ * candidate concurrently, as in a step), choosing one setting per case
+ * from the total time. */
+les_status les_ensemble_autotune(les_ensemble* ens, const les_pcg_opts* opts, double* best_us);
+
 /* ---- options (no reference counterpart) --------------------------------- */
 typedef enum les_option {
     LES_OPT_FUSED = 0,  /* mixed-precision inner iteration (Jacobi, Chebyshev degree

@@ -28,6 +28,8 @@ UNITS = {
     "les_mixed.cu": [],
     "les_fused.cu": [],
     "les_col.cu": [],
+    "les_ensemble.cu": [],
+    "les_tune.cu": [],
     "les_step.cu": ["-fmad=false"],
     "les_noalloc.cu": ["-fmad=false"],
 }

@@ -401,7 +401,8 @@ ColMap col_map(les_ctx* c, const void* fn, int halo, int tj, int ci_force)
     if (ci <= 0) {
         int occ = 1;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, CT, 0);
-        const long long warps = (long long)(occ < 1 ? 1 : occ) * CWPB * c->sms;
+        const double share = c->share > 0 && c->share <= 1 ? c->share : 1.0;
+        const long long warps = (long long)((occ < 1 ? 1 : occ) * CWPB * c->sms * share);
         long long chunks = warps / tiles;
         if (chunks < 1) chunks = 1;
         ci = (int)((g.nx + chunks - 1) / chunks);

@@ -273,6 +273,8 @@ struct les_ctx {
     int opt_tma = 0;              // LES_OPT_TMA: TMA-staged fused passes where the grid allows
     int tune_cia = 0, tune_cib = 0, tune_s = -1;   // autotuned march chunk lengths (0: occupancy rule)
     int tune_tja = 0, tune_tjb = 0;                // autotuned strip rows of the column passes (0: default)
+    double share = 1.0;           // fraction of the GPU's resident warps the column passes size
+                                  // their chunks for (1/k when k cases run together)
     struct les::TmaCache* tma = nullptr;
     les::StencilCoef coef{};
     double* L[7] = {};
@@ -354,6 +356,13 @@ les_status check_launch(les_ctx* c, const char* what);
 StencilView stencil_view(const les_ctx* c);
 les_status ensure_work(les_ctx* c);
 les_status ensure_work32(les_ctx* c);
+
+// graph-captured time steps (les_step.cu)
+bool graph_eligible(const les_ctx* c, const les_step_params* prm);
+les_status emit_step(les_ctx* c, const les_step_params* prm);   // into the capture on c->stream
+void swap_velocity(les_ctx* c);
+unsigned long long graph_step_stats(les_ctx* c, const les_step_params* prm, unsigned long long captured,
+                                    les_step_stats* stats);
 les_status read_state(les_ctx* c);
 int reduction_blocks(const Geo& g);
 

@@ -48,13 +48,42 @@ void step_graph_free(StepGraph* s)
     delete s;
 }
 
-}  // namespace les
-
-static bool graph_eligible(const les_ctx* c, const les_step_params* prm)
+bool graph_eligible(const les_ctx* c, const les_step_params* prm)
 {
-    return c->graph_on && !c->prof_on && prm->solver == LES_SOLVER_PCG && prm->pcg.precision == LES_MIXED &&
+    return !c->prof_on && prm->solver == LES_SOLVER_PCG && prm->pcg.precision == LES_MIXED &&
            c->stencil_mode == 1 && c->fused && fused_supported(&prm->pcg) && prm->pcg.max_iter > 0;
 }
+
+void swap_velocity(les_ctx* c)
+{
+    std::swap(c->slot[LES_U], c->slot[LES_U_NEW]);
+    std::swap(c->slot[LES_V], c->slot[LES_V_NEW]);
+    std::swap(c->slot[LES_W], c->slot[LES_W_NEW]);
+}
+
+// Statistics of the step a graph ran, from the device state (after a sync);
+// returns the number of kernels that ran (captured = the kernels captured:
+// those outside the loops and one pass of each loop body).
+unsigned long long graph_step_stats(les_ctx* c, const les_step_params* prm, unsigned long long captured,
+                                    les_step_stats* stats)
+{
+    const SolverState& o = c->h_state[0];
+    les_step_stats s{};
+    s.dt = prm->dt_fixed > 0 ? prm->dt_fixed : o.scal[0];
+    s.iters = o.iters;
+    s.outer = o.k;
+    s.residual = o.err;
+    s.b_norm = o.bnorm;
+    s.status = o.done ? (les_status)o.status : LES_NOT_CONVERGED;
+    if (stats) *stats = s;
+    // less one pass of each loop body (13 nodes), plus 8 kernels per outer
+    // correction and 5 per pass of the two-iteration inner body
+    const long long body = (o.iters - o.k + 1) / 2;
+    const long long run = (long long)captured - 13 + 8LL * o.k + 5LL * (body > 0 ? body : 0);
+    return run > 0 ? (unsigned long long)run : captured;
+}
+
+}  // namespace les
 
 static bool graph_matches(const les_ctx* c, const StepGraph* s, const les_step_params* prm)
 {
@@ -63,7 +92,7 @@ static bool graph_matches(const les_ctx* c, const StepGraph* s, const les_step_p
 }
 
 // One step (src/main.cpp:115-144) into the capture in progress on c->stream.
-static les_status emit_step(les_ctx* c, const les_step_params* prm)
+les_status les::emit_step(les_ctx* c, const les_step_params* prm)
 {
     les_status st;
     double dt = prm->dt_fixed;
@@ -126,31 +155,13 @@ static les_status step_graph(les_ctx* c, const les_step_params* prm, les_step_st
     st = check_cuda(c, cudaGraphLaunch(g->exec, c->stream), "launch step graph");
     if (st) return st;
     c->sg_last = g == c->sg[0] ? 0 : 1;
-    if (!fresh) {   // the captured momentum update swapped the buffers on the host only once
-        std::swap(c->slot[LES_U], c->slot[LES_U_NEW]);
-        std::swap(c->slot[LES_V], c->slot[LES_V_NEW]);
-        std::swap(c->slot[LES_W], c->slot[LES_W_NEW]);
-    }
+    if (!fresh) swap_velocity(c);   // the capture swapped the host pointers once; a replay must too
     if (!stats) {
         c->launches += g->captured;
         return LES_OK;
     }
     if ((st = read_state(c))) return st;
-    const SolverState& o = c->h_state[0];
-    les_step_stats s{};
-    s.dt = prm->dt_fixed > 0 ? prm->dt_fixed : o.scal[0];
-    s.iters = o.iters;
-    s.outer = o.k;
-    s.residual = o.err;
-    s.b_norm = o.bnorm;
-    s.status = o.done ? (les_status)o.status : LES_NOT_CONVERGED;
-    *stats = s;
-    // kernels run: the captured nodes, less one pass of each loop body (13
-    // nodes), plus 8 per outer correction and 5 per pass of the two-iteration
-    // inner body
-    const long long body = (o.iters - o.k + 1) / 2;
-    const long long run = (long long)g->captured - 13 + 8LL * o.k + 5LL * (body > 0 ? body : 0);
-    c->launches += run > 0 ? (unsigned long long)run : g->captured;
+    c->launches += graph_step_stats(c, prm, g->captured, stats);
     return LES_OK;
 }
 
@@ -161,7 +172,7 @@ extern "C" les_status les_step(les_ctx* c, const les_step_params* prm, les_step_
     if (prm->solver == LES_SOLVER_PCG && !c->stencil_mode)
         return fail(c, LES_BAD_ARG, "PCG needs a matrix: call les_build_stencil first");
     cudaSetDevice(c->device);
-    if (graph_eligible(c, prm)) return step_graph(c, prm, stats);
+    if (c->graph_on && graph_eligible(c, prm)) return step_graph(c, prm, stats);
     les_status st;
     double dt = prm->dt_fixed;
     if (!(dt > 0)) {

@@ -142,11 +142,6 @@ class Context:
             raise LesError(st, self.lib.les_status_string(st).decode())
         self.h = h
 
-    def close(self):
-        if self.h:
-            self.lib.les_destroy(self.h)
-            self.h = None
-
     def __del__(self):
         try:
             self.close()
@@ -360,3 +355,89 @@ class Context:
             if n:
                 out[self.lib.les_profile_name(kid).decode()] = (n, ms)
         return out
+
+    # --- autotuner
+    def autotune(self, opts, share=1.0):
+        """Times strip shapes and chunk lengths of the column passes for opts
+        and keeps the fastest; returns microseconds per inner iteration."""
+        us = C.c_double()
+        self.lib.les_autotune.argtypes = [C.c_void_p, C.POINTER(PcgOpts), C.c_double, C.POINTER(C.c_double)]
+        self._chk(self.lib.les_autotune(self.h, C.byref(opts), C.c_double(share), C.byref(us)))
+        return us.value
+
+    @classmethod
+    def borrowed(cls, handle, mesh, lib):
+        """A view of a context owned elsewhere (an ensemble case)."""
+        self = cls.__new__(cls)
+        self.lib, self.mesh, self.n, self.h = lib, mesh, mesh.n, C.c_void_p(handle)
+        self._borrowed = True
+        return self
+
+    def close(self):
+        if self.h and not getattr(self, "_borrowed", False):
+            self.lib.les_destroy(self.h)
+        self.h = None
+
+
+class Ensemble:
+    """Independent cases advanced by one CUDA graph launch per time step."""
+
+    def __init__(self, meshes, device=0, lib=None):
+        self.lib = L = lib or load()
+        L.les_ensemble_create.argtypes = [C.POINTER(Mesh), C.c_int, C.c_int, C.POINTER(C.c_void_p)]
+        L.les_ensemble_destroy.argtypes = [C.c_void_p]
+        L.les_ensemble_case.argtypes = [C.c_void_p, C.c_int]
+        L.les_ensemble_case.restype = C.c_void_p
+        L.les_ensemble_last_error.argtypes = [C.c_void_p]
+        L.les_ensemble_last_error.restype = C.c_char_p
+        L.les_ensemble_step.argtypes = [C.c_void_p, C.POINTER(StepParams), C.POINTER(StepStats)]
+        L.les_ensemble_sync.argtypes = [C.c_void_p]
+        L.les_ensemble_autotune.argtypes = [C.c_void_p, C.POINTER(PcgOpts), C.POINTER(C.c_double)]
+        self.n = len(meshes)
+        arr = (Mesh * self.n)(*meshes)
+        h = C.c_void_p()
+        st = L.les_ensemble_create(arr, self.n, device, C.byref(h))
+        if st != OK:
+            raise LesError(st, L.les_status_string(st).decode())
+        self.h = h
+        self.cases = [Context.borrowed(L.les_ensemble_case(h, i), meshes[i], L) for i in range(self.n)]
+
+    def _chk(self, st):
+        if st != OK:
+            raise LesError(st, self.lib.les_ensemble_last_error(self.h).decode())
+
+    def step(self, params, stats=True):
+        prm = (StepParams * self.n)(*params)
+        if not stats:
+            self._chk(self.lib.les_ensemble_step(self.h, prm, None))
+            return None
+        out = (StepStats * self.n)()
+        self._chk(self.lib.les_ensemble_step(self.h, prm, out))
+        return list(out)
+
+    def sync(self):
+        self._chk(self.lib.les_ensemble_sync(self.h))
+
+    def autotune(self, opts):
+        us = C.c_double()
+        self._chk(self.lib.les_ensemble_autotune(self.h, C.byref(opts), C.byref(us)))
+        return us.value
+
+    def close(self):
+        if self.h:
+            for c in self.cases:
+                c.h = None
+            self.lib.les_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

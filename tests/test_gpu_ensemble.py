@@ -1,0 +1,98 @@
+"""Batched ensemble (one CUDA graph launch per step for many ragged cases) and
+the autotuner of the fused inner passes.
+
+An ensemble case runs exactly the kernels of the same case stepped alone
+through les_step (graph mode), so fields and statistics must be identical."""
+import numpy as np
+import pytest
+
+from conftest import maxrel, same
+
+import les_cases
+import les_gb300 as G
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(c, spec):
+    shape = spec["shape"]
+    n = int(np.prod(shape))
+    c.upload_mask(np.zeros(n, np.uint8))
+    c.build_stencil()          # the reference's order: matrix before the obstacle
+    lmax = c.lambda_max(20)
+    solid = les_cases.box_mask(shape, spec["box"])
+    f = les_cases.init_fields(shape, spec["noise"], spec["seed"])
+    les_cases.velocity_bcs_np(shape, f, solid)
+    c.upload_fields(f)
+    c.upload_mask(solid)
+    return lmax
+
+
+def _params(spec, lmax):
+    return G.step_params(nu=les_cases.NU, rho=les_cases.RHO, cs=spec["cs"], cfl_conv=les_cases.CFL_CONV,
+                         solver=G.SOLVER_PCG, rel_tol=1e-8,
+                         pcg=G.pcg_opts(precond=G.PC_CHEBYSHEV, max_iter=5000, lambda_min=3 * np.pi ** 2,
+                                        lambda_max=lmax, degree=4, precision=G.MIXED, inner_rtol=1e-4))
+
+
+def _specs(count, seed):
+    specs = les_cases.batch_cases(count, seed)
+    for s in specs:   # keep the test quick: the two smallest extents of the ensemble's range
+        s["shape"] = tuple(min(d, 48) for d in s["shape"])
+        side = min(s["shape"]) // 4
+        s["box"] = (2, 2 + side, 2, 2 + side, 3, 3 + side)
+    return specs
+
+
+def _mesh(spec):
+    h = spec["h"]
+    return G.Mesh(*spec["shape"], h, h, h)
+
+
+def test_ensemble_matches_cases_stepped_alone():
+    specs = _specs(5, 11)
+    steps = 3
+    with G.Ensemble([_mesh(s) for s in specs]) as ens:
+        prm = [_params(s, _setup(c, s)) for c, s in zip(ens.cases, specs)]
+        est = [ens.step(prm) for _ in range(steps)]
+        efields = [c.download_fields() for c in ens.cases]
+    for i, s in enumerate(specs):
+        with G.Context(_mesh(s)) as c:
+            p = _params(s, _setup(c, s))
+            for k in range(steps):
+                st = c.step(p)
+                e = est[k][i]
+                assert (st.dt, st.iters, st.outer, st.residual, st.status) == \
+                       (e.dt, e.iters, e.outer, e.residual, e.status), (i, k)
+                assert st.status == G.OK and st.residual < 1e-8 * st.b_norm
+            f = c.download_fields()
+        for key in ("u", "v", "w", "p", "nu_t", "p_rhs"):
+            assert same(f[key], efields[i][key]), (i, key)
+
+
+def test_ensemble_autotune_keeps_the_solution():
+    specs = _specs(4, 23)
+    with G.Ensemble([_mesh(s) for s in specs]) as ens:
+        prm = [_params(s, _setup(c, s)) for c, s in zip(ens.cases, specs)]
+        us = ens.autotune(prm[0].pcg)
+        assert us > 0
+        stats = ens.step(prm)
+        tuned = [c.download("p") for c in ens.cases]
+    for i, s in enumerate(specs):
+        assert stats[i].status == G.OK and stats[i].residual < 1e-8 * stats[i].b_norm
+        with G.Context(_mesh(s)) as c:
+            p = _params(s, _setup(c, s))
+            c.step(p)
+            # another strip shape rounds the FP32 inner sums differently; the
+            # outer FP64 correction holds both to the mixed-vs-FP64 bar
+            assert maxrel(c.download("p"), tuned[i]) < 1e-6
+
+
+def test_autotune_single_context():
+    spec = dict(shape=(96, 48, 64), h=1.0 / 32, box=(20, 32, 10, 22, 20, 32), cs=0.17, seed=3, noise=0.01)
+    with G.Context(_mesh(spec)) as c:
+        p = _params(spec, _setup(c, spec))
+        us = c.autotune(p.pcg)
+        assert 0 < us < 1e5
+        st = c.step(p)
+        assert st.status == G.OK and st.residual < 1e-8 * st.b_norm
