@@ -55,7 +55,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
-    ap.add_argument("--workload", default="large", choices=("small", "large", "xlarge", "batch"))
+    ap.add_argument("--workload", default="large", choices=("small", "large", "xlarge", "batch", "adjoint"))
+    ap.add_argument("--adj-steps", type=int, default=50, help="adjoint workload: forward steps")
+    ap.add_argument("--fd-step", type=float, default=1e-6, help="adjoint workload: finite-difference step")
     ap.add_argument("--batch", type=int, default=64, help="cases of the batch workload")
     ap.add_argument("--tune", type=int, default=1, help="batch workload: run the ensemble autotuner first")
     ap.add_argument("--precond", default="cheb", choices=("cheb", "jacobi", "ic"))
@@ -334,6 +336,91 @@ def run_batch(args):
     return 0
 
 
+def run_adjoint(args):
+    """Adjoint workload: 128x64x64 (h = 1/64) with the centred cube, N steps
+    of the mixed-precision Chebyshev(4) step at fixed dt, J = time average of
+    the probe-box kinetic energy over [96,120)x[16,48)x[16,48); gradient with
+    respect to the 64x64 inlet u-profile (at the uniform profile u = 1) and
+    Cs, checkpoint every 10 steps; checked against central finite
+    differences (step --fd-step) on 16 seeded profile entries and on Cs."""
+    import torch
+    import les_cases
+    import les_gb300 as G
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(0)
+    shape, h, solid, f = les_cases.case("adjoint", args.seed)
+    n = int(np.prod(shape))
+    box = (96, 120, 16, 48, 16, 48)
+    nsteps = args.adj_steps
+    prof0 = np.ones(shape[1] * shape[2])
+
+    def setup(c, prof):
+        c.upload_mask(np.zeros(n, np.uint8))
+        c.build_stencil()
+        lmax = c.lambda_max(20)
+        c.upload_fields(f)
+        c.upload_mask(solid)
+        c.set_inlet(prof)
+        c.velocity_bcs()
+        dt = c.adaptive_dt(les_cases.NU, les_cases.CFL_CONV, les_cases.CFL_VISC, les_cases.DT_MAX)
+        return lmax, dt
+
+    def params(lmax, dt, cs):
+        return G.step_params(nu=les_cases.NU, rho=les_cases.RHO, cs=cs, dt_fixed=dt, solver=G.SOLVER_PCG,
+                             rel_tol=1e-12,
+                             pcg=G.pcg_opts(precond=G.PC_CHEBYSHEV, max_iter=50000, lambda_min=3 * np.pi ** 2,
+                                            lambda_max=lmax, degree=4, precision=G.MIXED, inner_rtol=1e-4))
+
+    mesh = G.Mesh(*shape, h, h, h)
+
+    def J_of(prof, cs):
+        with G.Context(mesh) as c:
+            lmax, dt = setup(c, prof)
+            return c.adjoint_forward(params(lmax, dt, cs), nsteps, 10, box, 1e-12)
+
+    with G.Context(mesh) as c:
+        lmax, dt = setup(c, prof0)
+        prm = params(lmax, dt, les_cases.CS)
+        c.sync()
+        t0 = time.perf_counter()
+        J = c.adjoint_forward(prm, nsteps, 10, box, 1e-12)
+        t_fwd = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        g, gcs = c.adjoint_backward()
+        t_bwd = time.perf_counter() - t0
+    rng = np.random.default_rng(args.seed)
+    ny, nz = shape[1], shape[2]
+    cand = [(j, k) for j in range(1, ny - 1) for k in range(1, nz - 1)]
+    pick = [cand[i] for i in rng.choice(len(cand), 16, replace=False)]
+    hs = args.fd_step
+    rows = []
+    for (j, k) in pick:
+        idx = j * nz + k
+        p1, p2 = prof0.copy(), prof0.copy()
+        p1[idx] += hs
+        p2[idx] -= hs
+        fd = (J_of(p1, les_cases.CS) - J_of(p2, les_cases.CS)) / (2 * hs)
+        rows.append({"j": j, "k": k, "adjoint": float(g[idx]), "fd": fd,
+                     "rel_err": abs(fd - g[idx]) / max(abs(g[idx]), 1e-300)})
+    fdc = (J_of(prof0, les_cases.CS + hs) - J_of(prof0, les_cases.CS - hs)) / (2 * hs)
+    cs_err = abs(fdc - gcs) / max(abs(gcs), 1e-300)
+    errs = [r["rel_err"] for r in rows] + [cs_err]
+    line = {"metric": "adjoint gradient of the probe-box kinetic energy vs central finite differences",
+            "value": max(errs), "unit": "max relative error", "higher_is_better": False, "n_gpus": 1,
+            "steps": nsteps, "warmup": 0, "dtype": "f32 inner / f64 outer (tol 1e-12)", "data": "synthetic",
+            "config": {"workload": "adjoint 128x64x64 h=1/64 centred cube, %d steps, dt %.3g fixed, checkpoint "
+                                   "every 10, probe [96,120)x[16,48)x[16,48), controls 64x64 inlet u + Cs" % (nsteps, dt),
+                       "fd_step": hs, "fd_entries": 16},
+            "J": J, "grad_cs": gcs, "fd_cs": fdc, "cs_rel_err": cs_err, "grad_inlet_max_abs": float(np.abs(g).max()),
+            "median_rel_err": float(np.median(errs)), "entries": rows,
+            "forward_s": t_fwd, "backward_s": t_bwd, "backward_over_forward": t_bwd / t_fwd}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_ours(args):
     import torch
     import les_cases
@@ -517,6 +604,8 @@ def main():
         return run_reference(args)
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "adjoint":
+        return run_adjoint(args)
     return run_ours(args)
 
 

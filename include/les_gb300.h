@@ -237,6 +237,35 @@ const char* les_ensemble_last_error(const les_ensemble* ens);
 les_status les_ensemble_step(les_ensemble* ens, const les_step_params* prm, les_step_stats* stats);
 les_status les_ensemble_sync(les_ensemble* ens);
 
+/* ---- adjoint (no reference counterpart) --------------------------------- */
+/* Inlet u profile (ny*nz values, index j*nz+k) applied by the velocity
+ * boundary conditions in place of the reference's uniform u = 1
+ * (src/main.cpp:334-345); NULL restores the uniform inlet. */
+les_status les_set_inlet(les_ctx* ctx, const double* u_in);
+
+/* Gradient of J = (1/N) sum_{n=1..N} sum_{probe box} |U_n|^2 / 2 (U_n the
+ * velocity after step n) with respect to the inlet profile and Cs, by the
+ * discrete adjoint of the time step (hand-written transposes of the SGS,
+ * momentum, divergence, projection and boundary-condition kernels; the
+ * adjoint pressure solve reuses the PCG through the symmetrising scaling of
+ * the matrix).  The forward starts from the context's current fields with the
+ * velocity boundary conditions applied (so the initial inlet values are the
+ * profile too), stores (u, v, w, p) every checkpoint_every steps, and the
+ * backward recomputes each segment from its checkpoint. */
+typedef struct les_adjoint_params {
+    les_step_params step;   /* PCG (Jacobi or Chebyshev; FP64, or mixed with its FP64
+                               defect correction for tight tolerances), dt_fixed > 0;
+                               the adjoint solves use the same solver */
+    int steps;              /* N */
+    int checkpoint_every;   /* steps per checkpoint segment */
+    int box[6];             /* probe box i0, i1, j0, j1, k0, k1 (half-open) */
+    double adj_rel_tol;     /* adjoint pressure solves: relative residual */
+} les_adjoint_params;
+les_status les_adjoint_forward(les_ctx* ctx, const les_adjoint_params* prm, double* J);
+/* grad_inlet: ny*nz values (dJ/du_in), grad_cs: dJ/dCs.  Leaves the fields
+ * at the first checkpoint's recomputation (restore them to continue). */
+les_status les_adjoint_backward(les_ctx* ctx, double* grad_inlet, double* grad_cs);
+
 /* ---- autotuner (no reference counterpart) ------------------------------- */
 /* Times the fused inner passes of the mixed-precision PCG for opts on the
  * context's current matrix over candidate strip shapes and march chunk

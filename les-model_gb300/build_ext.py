@@ -30,6 +30,7 @@ UNITS = {
     "les_col.cu": [],
     "les_ensemble.cu": [],
     "les_tune.cu": [],
+    "les_adjoint.cu": ["-fmad=false"],
     "les_step.cu": ["-fmad=false"],
     "les_noalloc.cu": ["-fmad=false"],
 }

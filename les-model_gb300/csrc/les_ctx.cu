@@ -196,6 +196,8 @@ void les_destroy(les_ctx* c)
     les::tma_cache_free(c->tma);
     les::step_graph_free(c->sg[0]);
     les::step_graph_free(c->sg[1]);
+    les::adj_work_free(c->adj);
+    cudaFree(c->inlet);
     if (c->aux) cudaStreamDestroy(c->aux);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;

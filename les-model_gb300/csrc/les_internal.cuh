@@ -23,6 +23,8 @@ struct TmaCache;                       // tensor maps of the fused passes (les_f
 void tma_cache_free(TmaCache* t);
 struct StepGraph;                      // captured time step (les_step.cu)
 void step_graph_free(StepGraph* s);
+struct AdjWork;                        // adjoint checkpoints and work vectors (les_adjoint.cu)
+void adj_work_free(AdjWork* a);
 
 // ---- geometry -------------------------------------------------------------
 struct Geo {
@@ -280,6 +282,8 @@ struct les_ctx {
     double* L[7] = {};
     bool have_L = false;
     double* tau = nullptr;
+    double* inlet = nullptr;      // inlet u profile (ny*nz) or nullptr for the reference's uniform 1
+    struct les::AdjWork* adj = nullptr;   // adjoint checkpoints and work (les_adjoint.cu)
     // work vectors (FP64)
     double* w[8] = {};
     // FP32 work vectors for the mixed-precision inner solve, and FP32 copies

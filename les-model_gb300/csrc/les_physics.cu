@@ -148,8 +148,10 @@ __global__ void k_zero_list3(const int* __restrict__ list, int n, double* a, dou
 //   i == nx-1 (j, k interior)           -> value of (nx-2, j, k) before the
 //                                          obstacle overwrite
 // The interior obstacle overwrite (:395-409) runs afterwards (k_zero_list3).
+// inlet != nullptr: the inlet u is the per-(j,k) profile inlet[j*nz+k]
+// (the adjoint's control) instead of the reference's uniform 1.
 __global__ void k_velocity_faces(Geo g, const uint8_t* __restrict__ solid, double* __restrict__ u,
-                                 double* __restrict__ v, double* __restrict__ w)
+                                 double* __restrict__ v, double* __restrict__ w, const double* __restrict__ inlet)
 {
     int i, j, k;
     if (!cell_coords(g, i, j, k)) return;
@@ -158,7 +160,7 @@ __global__ void k_velocity_faces(Geo g, const uint8_t* __restrict__ solid, doubl
     int id = i * g.si + j * g.sj + k;
     if (!jk_in) { u[id] = 0.0; v[id] = 0.0; w[id] = 0.0; return; }
     if (i == 0) {
-        if (!solid[id]) { u[id] = 1.0; v[id] = 0.0; w[id] = 0.0; }
+        if (!solid[id]) { u[id] = inlet ? inlet[j * g.nz + k] : 1.0; v[id] = 0.0; w[id] = 0.0; }
         return;
     }
     int src = id - g.si;
@@ -285,8 +287,8 @@ namespace les {
 les_status velocity_bcs_dev(les_ctx* c)
 {
     const Geo& g = c->g;
-    launch(c, k_velocity_faces, cell_grid(g), cell_block(), g, c->mask, c->slot[LES_U],
-                                                                    c->slot[LES_V], c->slot[LES_W]);
+    launch(c, k_velocity_faces, cell_grid(g), cell_block(), g, c->mask, c->slot[LES_U], c->slot[LES_V],
+           c->slot[LES_W], (const double*)c->inlet);
     if (c->n_solid)
         launch(c, k_zero_list3, (c->n_solid + 255) / 256, 256, 
             c->solid_list, c->n_solid, c->slot[LES_U], c->slot[LES_V], c->slot[LES_W]);

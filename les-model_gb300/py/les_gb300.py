@@ -65,6 +65,11 @@ class StepParams(C.Structure):
                 ("omega", C.c_double), ("want_tau", C.c_int)]
 
 
+class AdjointParams(C.Structure):
+    _fields_ = [("step", StepParams), ("steps", C.c_int), ("checkpoint_every", C.c_int),
+                ("box", C.c_int * 6), ("adj_rel_tol", C.c_double)]
+
+
 class StepStats(C.Structure):
     _fields_ = [("dt", C.c_double), ("iters", C.c_int), ("outer", C.c_int),
                 ("residual", C.c_double), ("b_norm", C.c_double), ("status", C.c_int)]
@@ -441,3 +446,35 @@ class Ensemble:
 
     def __exit__(self, *a):
         self.close()
+
+
+def _ctx_set_inlet(self, u_in):
+    """Inlet u profile (ny*nz, index j*nz+k) or None for the uniform inlet."""
+    self.lib.les_set_inlet.argtypes = [C.c_void_p, C.c_void_p]
+    if u_in is None:
+        self._chk(self.lib.les_set_inlet(self.h, None))
+    else:
+        a = _arr(u_in)
+        assert a.size == self.mesh.ny * self.mesh.nz
+        self._chk(self.lib.les_set_inlet(self.h, a.ctypes.data))
+
+
+def _ctx_adjoint_forward(self, step, steps, checkpoint_every, box, adj_rel_tol=1e-12):
+    p = AdjointParams(step, steps, checkpoint_every, (C.c_int * 6)(*box), adj_rel_tol)
+    J = C.c_double()
+    self.lib.les_adjoint_forward.argtypes = [C.c_void_p, C.POINTER(AdjointParams), C.POINTER(C.c_double)]
+    self._chk(self.lib.les_adjoint_forward(self.h, C.byref(p), C.byref(J)))
+    return J.value
+
+
+def _ctx_adjoint_backward(self):
+    g = np.zeros(self.mesh.ny * self.mesh.nz)
+    gcs = C.c_double()
+    self.lib.les_adjoint_backward.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]
+    self._chk(self.lib.les_adjoint_backward(self.h, g.ctypes.data, C.byref(gcs)))
+    return g, gcs.value
+
+
+Context.set_inlet = _ctx_set_inlet
+Context.adjoint_forward = _ctx_adjoint_forward
+Context.adjoint_backward = _ctx_adjoint_backward

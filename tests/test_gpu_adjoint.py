@@ -1,0 +1,88 @@
+"""Discrete adjoint of the time step: gradients of the time-averaged probe-box
+kinetic energy with respect to the inlet u-profile and Cs, against central
+finite differences of the forward model, and independent of the checkpoint
+interval (the backward sweep recomputes each segment exactly)."""
+import numpy as np
+import pytest
+
+import les_cases
+import les_gb300 as G
+
+pytestmark = pytest.mark.gpu
+
+SHAPE = (24, 12, 12)
+H = 1.0 / 32
+BOX = (2, 10, 2, 10, 2, 10)
+STEPS = 6
+
+
+def _setup(c, profile, seed=4):
+    n = int(np.prod(SHAPE))
+    c.upload_mask(np.zeros(n, np.uint8))
+    c.build_stencil()
+    lmax = c.lambda_max(20)
+    solid = les_cases.box_mask(SHAPE, (14, 17, 5, 8, 5, 8))
+    f = les_cases.init_fields(SHAPE, 0.05, seed)
+    c.upload_fields(f)
+    c.upload_mask(solid)
+    c.set_inlet(profile)
+    c.velocity_bcs()
+    return lmax
+
+
+def _params(lmax, cs):
+    # mixed precision: the FP64 defect correction reaches a relative residual
+    # of 1e-12 where CG on the non-symmetric FP64 system stalls
+    return G.step_params(nu=1e-4, rho=les_cases.RHO, cs=cs, dt_fixed=4e-3, solver=G.SOLVER_PCG, rel_tol=1e-12,
+                         pcg=G.pcg_opts(precond=G.PC_CHEBYSHEV, max_iter=20000, lambda_min=3 * np.pi ** 2,
+                                        lambda_max=lmax, degree=4, precision=G.MIXED, inner_rtol=1e-4))
+
+
+def _J(profile, cs):
+    with G.Context(G.Mesh(*SHAPE, H, H, H)) as c:
+        lmax = _setup(c, profile)
+        return c.adjoint_forward(_params(lmax, cs), STEPS, STEPS, BOX)
+
+
+def _grad(profile, cs, every):
+    with G.Context(G.Mesh(*SHAPE, H, H, H)) as c:
+        lmax = _setup(c, profile)
+        J = c.adjoint_forward(_params(lmax, cs), STEPS, every, BOX)
+        g, gcs = c.adjoint_backward()
+        return J, g, gcs
+
+
+def _profile():
+    rng = np.random.default_rng(9)
+    return 1.0 + 0.1 * rng.standard_normal(SHAPE[1] * SHAPE[2])
+
+
+def test_adjoint_gradient_matches_finite_differences():
+    prof, cs = _profile(), 0.17
+    J, g, gcs = _grad(prof, cs, 4)
+    assert J > 0 and np.all(np.isfinite(g)) and np.isfinite(gcs)
+    ny, nz = SHAPE[1], SHAPE[2]
+    gi = g.reshape(ny, nz)
+    assert np.all(gi[0, :] == 0) and np.all(gi[:, 0] == 0)   # wall cells are not controls
+    # the four largest inlet sensitivities and Cs, central differences
+    order = np.argsort(-np.abs(g))[:4]
+    h = 1e-5
+    for idx in order:
+        p1, p2 = prof.copy(), prof.copy()
+        p1[idx] += h
+        p2[idx] -= h
+        fd = (_J(p1, cs) - _J(p2, cs)) / (2 * h)
+        assert abs(fd - g[idx]) <= 1e-5 * abs(g[idx]), (idx, fd, g[idx])
+    hc = 1e-5
+    fd = (_J(prof, cs + hc) - _J(prof, cs - hc)) / (2 * hc)
+    assert abs(fd - gcs) <= 1e-5 * abs(gcs), (fd, gcs)
+
+
+def test_adjoint_is_independent_of_the_checkpoint_interval():
+    prof, cs = _profile(), 0.15
+    J1, g1, c1 = _grad(prof, cs, 1)
+    J4, g4, c4 = _grad(prof, cs, 4)
+    J6, g6, c6 = _grad(prof, cs, STEPS)
+    assert J1 == J4 == J6
+    assert np.array_equal(g1, g4) and np.array_equal(g4, g6)
+    assert c1 == c4 == c6
