@@ -62,6 +62,7 @@ struct StripPos {
     int i0, i1;    // owned planes [i0, i1)
     int kl;        // this lane's k after reflection at the walls (-1: not loaded)
     unsigned own;  // bit r: cell of row r owned by this lane
+    bool jin;      // every row of the strip inside the grid: rows need no reflection
 };
 
 // reflection of index x into [0, n) about the end cells (-1 if still outside)
@@ -80,6 +81,7 @@ __device__ __forceinline__ StripPos strip_pos(const Geo& g, const ColMap& m, int
     const int jt = rest % m.tiles_j, ch = rest / m.tiles_j;
     const int kg = kt * m.tk - HALO + lane;
     s.j0 = jt * TJ - HALO;
+    s.jin = s.j0 >= 0 && s.j0 + TJ + 2 * HALO <= g.ny;
     s.i0 = ch * m.ci;
     s.i1 = min(g.nx, s.i0 + m.ci);
     s.kl = reflect(kg, g.nz);
@@ -124,6 +126,18 @@ __global__ void __launch_bounds__(CT, TJ == 8 ? 4 : 2) k_col_a(Geo g, ColMap m, 
         for (int r = 0; r < H; ++r) p0[r] = p1[r] = p2[r] = 0.f;
         auto fetch = [&](int P) {
             const bool pown = P >= s.i0 && P < s.i1;
+            if (s.jin) {   // interior row strip: consecutive rows, one validity test
+                const int pl = P < 0 ? -P : P;
+                const bool ok = s.kl >= 0 && pl < g.nx;
+                int id = pl * g.si + s.j0 * g.sj + s.kl;
+#pragma unroll
+                for (int r = 0; r < H; ++r, id += g.sj) {
+                    vz[r] = ok ? z[id] : 0.f;
+                    vp[r] = (!FIRST && ok) ? pold[id] : 0.f;
+                    if (r >= 1 && r <= TJ) ve[r - 1] = (!FIRST && pown && ((s.own >> r) & 1u)) ? e[id] : 0.f;
+                }
+                return;
+            }
 #pragma unroll
             for (int r = 0; r < H; ++r) {
                 const int id = row_off(g, s, P, r);
@@ -152,8 +166,12 @@ __global__ void __launch_bounds__(CT, TJ == 8 ? 4 : 2) k_col_a(Geo g, ColMap m, 
             const int C = P - 1;
             if (C >= s.i0) {
                 const int cb = C * g.si + s.j0 * g.sj + s.kl;
-                const bool ident = C == g.nx - 1;           // outlet plane: identity row
-                const float ex = C == g.nx - 2 ? 0.f : k.x1; // no east coefficient before the outlet
+                // plane-uniform coefficients: the outlet plane is an identity
+                // row, the plane before it has no east coefficient
+                const bool ident = C == g.nx - 1;
+                const float cc = ident ? 1.f : k.c0, cx = ident ? 0.f : k.x1;
+                const float ce = (ident || C == g.nx - 2) ? 0.f : k.x1;
+                const float cy = ident ? 0.f : k.y1, cz = ident ? 0.f : k.z1;
                 float sq = 0.f;
 #pragma unroll
                 for (int r = 1; r <= TJ; ++r) {
@@ -161,9 +179,8 @@ __global__ void __launch_bounds__(CT, TJ == 8 ? 4 : 2) k_col_a(Geo g, ColMap m, 
                     const float pb = __shfl_up_sync(FULL, pc, 1);
                     const float pt = __shfl_down_sync(FULL, pc, 1);
                     if ((s.own >> r) & 1u) {
-                        float val = k.c0 * pc + k.x1 * p2[r] + ex * p0[r] + k.y1 * (p1[r - 1] + p1[r + 1]) +
-                                    k.z1 * (pb + pt);
-                        val = ident ? pc : val;
+                        const float val = cc * pc + cx * p2[r] + ce * p0[r] + cy * (p1[r - 1] + p1[r + 1]) +
+                                          cz * (pb + pt);
                         q[cb + r * g.sj] = val;
                         sq = fmaf(pc, val, sq);
                     }
@@ -220,6 +237,17 @@ __global__ void __launch_bounds__(CT, (TJ == 4 && S <= 3) ? 3 : 2) k_col_b(Geo g
                 pcr[L][0][r] = pcr[L][1][r] = 0.f;
             }
         auto fetch = [&](int P) {
+            if (s.jin) {   // interior row strip: consecutive rows, one validity test
+                const int pl = P < 0 ? -P : P;
+                const bool ok = s.kl >= 0 && pl < g.nx;
+                int id = pl * g.si + s.j0 * g.sj + s.kl;
+#pragma unroll
+                for (int r = 0; r < H; ++r, id += g.sj) {
+                    vr[r] = ok ? r_in[id] : 0.f;
+                    vq[r] = (!FIRST && ok) ? q[id] : 0.f;
+                }
+                return;
+            }
 #pragma unroll
             for (int r = 0; r < H; ++r) {
                 const int id = row_off(g, s, P, r);
@@ -261,8 +289,14 @@ __global__ void __launch_bounds__(CT, (TJ == 4 && S <= 3) ? 3 : 2) k_col_b(Geo g
             for (int LV = 1; LV <= S; ++LV) {
                 const int Pk = I - LV;
                 const float ak = cf.a[LV - 1], bk = cf.b[LV - 1];
+                // plane-uniform coefficients: the outlet plane is an identity
+                // row, the plane before it has no east coefficient; level 1
+                // applies A to z_0 = a0 r', so a0 is folded in
                 const bool ident = Pk == g.nx - 1;
-                const float ex = Pk == g.nx - 2 ? 0.f : k.x1;
+                const float sc = LV == 1 ? cf.a0 : 1.f;
+                const float cc = sc * (ident ? 1.f : k.c0), cx = ident ? 0.f : sc * k.x1;
+                const float ce = (ident || Pk == g.nx - 2) ? 0.f : sc * k.x1;
+                const float cy = ident ? 0.f : sc * k.y1, cz = ident ? 0.f : sc * k.z1;
                 const bool out_plane = LV == S && Pk >= s.i0 && Pk < s.i1;
                 const int pbase = Pk * g.si + s.j0 * g.sj + s.kl;
                 float s2 = 0.f;
@@ -280,12 +314,8 @@ __global__ void __launch_bounds__(CT, (TJ == 4 && S <= 3) ? 3 : 2) k_col_b(Geo g
                     }
                     const float zb = __shfl_up_sync(FULL, zc, 1);
                     const float zt = __shfl_down_sync(FULL, zc, 1);
-                    float az = k.c0 * zc + k.x1 * zw + ex * ze + k.y1 * (zs + zn) + k.z1 * (zb + zt);
-                    az = ident ? zc : az;
-                    if (LV == 1) {
-                        az *= cf.a0;
-                        zc *= cf.a0;
-                    }
+                    const float az = cc * zc + cx * zw + ce * ze + cy * (zs + zn) + cz * (zb + zt);
+                    if (LV == 1) zc *= cf.a0;
                     const float rv = rp[LV][r];
                     const float pck = fmaf(bk, pcp, rv - az);
                     const float zk = fmaf(ak, pck, zc);
