@@ -237,6 +237,48 @@ const char* les_ensemble_last_error(const les_ensemble* ens);
 les_status les_ensemble_step(les_ensemble* ens, const les_step_params* prm, les_step_stats* stats);
 les_status les_ensemble_sync(les_ensemble* ens);
 
+/* ---- statistics (src/statistics.cpp) ------------------------------------ */
+/* init_statistics (:80-96): zeroes the ten device-resident sums. */
+les_status les_stats_begin(les_ctx* ctx, int start_step);
+/* update_statistics (:98-131): adds the current u, v, w, p (and their
+ * products) when current_step > start_step; no host copy. */
+les_status les_stats_update(les_ctx* ctx, int current_step);
+/* The raw sums (u, v, w, p, uu, vv, ww, uv, uw, vw; entries may be NULL). */
+les_status les_stats_sums(les_ctx* ctx, double* const* out10, int* samples);
+/* finalize_and_save (:133-186) without the file: means u, v, w, p and the
+ * stresses uu, vv, ww, uv, uw, vw into out10 (entries may be NULL). */
+les_status les_stats_finalize(les_ctx* ctx, double* const* out10, int* samples);
+/* finalize_and_save: the statistics file (write_statistics_vtk, :11-71). */
+les_status les_stats_save_vtk(les_ctx* ctx, const char* path);
+
+/* ---- files (src/io.cpp) ---------------------------------------------------- */
+/* write_field_vtk (:225-256) of the context's fields into `path` (the
+ * reference's name is output/output_<step>.vtk).  Asynchronous: the fields
+ * are snapshot on the device, staged to pinned memory on a copy stream and
+ * formatted on host threads while the caller continues; les_io_wait joins. */
+les_status les_write_vtk(les_ctx* ctx, int step, const char* path);
+/* save_state (:14-58) into dir/checkpoint.meta and dir/checkpoint.data (the
+ * reference's dir is "checkpoint"), asynchronous like les_write_vtk.
+ * with_unew = 1 also writes u_new, v_new, w_new to dir/checkpoint.unew (not
+ * in the reference's format: it makes a resume exact). */
+les_status les_save_state(les_ctx* ctx, const char* dir, double time_simulated, double dt, int next_step,
+                          int with_unew);
+/* Waits for the last asynchronous file; returns its status. */
+les_status les_io_wait(les_ctx* ctx);
+/* load_state (:73-120): *step = 0 when dir holds no checkpoint. */
+les_status les_load_state(les_ctx* ctx, const char* dir, double* time_simulated, double* dt, int* step,
+                          int with_unew);
+/* The same formats from host arrays (no device involved). */
+les_status les_format_field_vtk(const les_mesh* mesh, int step, const double* u, const double* v, const double* w,
+                                const double* p, const double* nu_t, const uint8_t* solid, const char* path);
+les_status les_format_stats_vtk(const les_mesh* mesh, const double* const* mean4, const double* const* stress6,
+                                const char* path);
+les_status les_write_checkpoint_files(const les_mesh* mesh, const double* const* fields5, const uint8_t* solid,
+                                      double time_simulated, double dt, int next_step, const char* dir,
+                                      const double* const* unew3);
+les_status les_read_checkpoint_files(const les_mesh* mesh, const char* dir, double* const* fields5, uint8_t* solid,
+                                     double* time_simulated, double* dt, int* step, double* const* unew3);
+
 /* ---- adjoint (no reference counterpart) --------------------------------- */
 /* Inlet u profile (ny*nz values, index j*nz+k) applied by the velocity
  * boundary conditions in place of the reference's uniform u = 1

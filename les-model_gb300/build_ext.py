@@ -31,6 +31,7 @@ UNITS = {
     "les_ensemble.cu": [],
     "les_tune.cu": [],
     "les_adjoint.cu": ["-fmad=false"],
+    "les_io.cu": ["-fmad=false"],
     "les_step.cu": ["-fmad=false"],
     "les_noalloc.cu": ["-fmad=false"],
 }
@@ -77,7 +78,7 @@ def build(force=False, verbose=False, extra=()):
     with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         objs = list(ex.map(one, sorted(UNITS)))
     tmp = LIB + ".tmp%d" % os.getpid()
-    cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs]
+    cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lpthread"]
     p = subprocess.run(cmd, capture_output=True, text=True)
     if p.returncode:
         sys.stderr.write(" ".join(cmd) + "\n" + p.stdout + p.stderr)

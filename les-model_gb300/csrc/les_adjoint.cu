@@ -429,6 +429,13 @@ les_status step_adjoint(les_ctx* c, AdjWork& a)
     if (rr > 0.0) {
         les_pcg_opts o = p.pcg;
         o.tol = a.prm.adj_rel_tol * std::sqrt(rr);
+        if (o.precision == LES_MIXED) {
+            // an inner FP32 CG that stagnates on this non-symmetric system
+            // ends after a bounded number of iterations; the FP64 outer
+            // correction carries on from what it reached
+            if (o.inner_max_iter <= 0) o.inner_max_iter = 400;
+            if (o.max_outer < 200) o.max_outer = 200;
+        }
         double* sb = c->slot[LES_B];
         double* sp = c->slot[LES_P];
         c->slot[LES_B] = a.lp;

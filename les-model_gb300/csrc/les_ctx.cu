@@ -197,6 +197,7 @@ void les_destroy(les_ctx* c)
     les::step_graph_free(c->sg[0]);
     les::step_graph_free(c->sg[1]);
     les::adj_work_free(c->adj);
+    les::io_work_free(c->io);   // joins a file writer still running
     cudaFree(c->inlet);
     if (c->aux) cudaStreamDestroy(c->aux);
     if (c->stream) cudaStreamDestroy(c->stream);

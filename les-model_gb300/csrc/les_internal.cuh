@@ -25,6 +25,8 @@ struct StepGraph;                      // captured time step (les_step.cu)
 void step_graph_free(StepGraph* s);
 struct AdjWork;                        // adjoint checkpoints and work vectors (les_adjoint.cu)
 void adj_work_free(AdjWork* a);
+struct IoWork;                         // statistics sums, file staging and writer thread (les_io.cu)
+void io_work_free(IoWork* w);
 
 // ---- geometry -------------------------------------------------------------
 struct Geo {
@@ -284,6 +286,7 @@ struct les_ctx {
     double* tau = nullptr;
     double* inlet = nullptr;      // inlet u profile (ny*nz) or nullptr for the reference's uniform 1
     struct les::AdjWork* adj = nullptr;   // adjoint checkpoints and work (les_adjoint.cu)
+    struct les::IoWork* io = nullptr;     // statistics and file output (les_io.cu)
     // work vectors (FP64)
     double* w[8] = {};
     // FP32 work vectors for the mixed-precision inner solve, and FP32 copies

@@ -478,3 +478,108 @@ def _ctx_adjoint_backward(self):
 Context.set_inlet = _ctx_set_inlet
 Context.adjoint_forward = _ctx_adjoint_forward
 Context.adjoint_backward = _ctx_adjoint_backward
+
+
+# ---- statistics and files (src/statistics.cpp, src/io.cpp)
+_STAT_KEYS = ("u", "v", "w", "p", "uu", "vv", "ww", "uv", "uw", "vw")
+
+
+def _ptr_array(arrs):
+    return (C.POINTER(C.c_double) * len(arrs))(*[None if a is None else a.ctypes.data_as(_dp) for a in arrs])
+
+
+def _ctx_stats_begin(self, start_step):
+    self._chk(self.lib.les_stats_begin(self.h, int(start_step)))
+
+
+def _ctx_stats_update(self, step):
+    self._chk(self.lib.les_stats_update(self.h, int(step)))
+
+
+def _ctx_stats_read(self, finalize=False):
+    out = [np.empty(self.n) for _ in range(10)]
+    ns = C.c_int()
+    fn = self.lib.les_stats_finalize if finalize else self.lib.les_stats_sums
+    self._chk(fn(self.h, _ptr_array(out), C.byref(ns)))
+    return dict(zip(_STAT_KEYS, out)), ns.value
+
+
+def _ctx_stats_save_vtk(self, path):
+    self._chk(self.lib.les_stats_save_vtk(self.h, str(path).encode()))
+
+
+def _ctx_write_vtk(self, step, path):
+    self._chk(self.lib.les_write_vtk(self.h, int(step), str(path).encode()))
+
+
+def _ctx_save_state(self, d, time_simulated, dt, next_step, with_unew=False):
+    self._chk(self.lib.les_save_state(self.h, str(d).encode(), C.c_double(time_simulated), C.c_double(dt),
+                                      int(next_step), int(with_unew)))
+
+
+def _ctx_io_wait(self):
+    self._chk(self.lib.les_io_wait(self.h))
+
+
+def _ctx_load_state(self, d, with_unew=False):
+    t, dt, step = C.c_double(), C.c_double(), C.c_int()
+    self._chk(self.lib.les_load_state(self.h, str(d).encode(), C.byref(t), C.byref(dt), C.byref(step),
+                                      int(with_unew)))
+    return step.value, t.value, dt.value
+
+
+Context.stats_begin = _ctx_stats_begin
+Context.stats_update = _ctx_stats_update
+Context.stats_read = _ctx_stats_read
+Context.stats_save_vtk = _ctx_stats_save_vtk
+Context.write_vtk = _ctx_write_vtk
+Context.save_state = _ctx_save_state
+Context.io_wait = _ctx_io_wait
+Context.load_state = _ctx_load_state
+
+
+def format_field_vtk(mesh, step, f, solid, path, lib=None):
+    """write_field_vtk from host arrays (no device)."""
+    L = lib or load()
+    a = [_arr(f[k]) for k in ("u", "v", "w", "p", "nu_t")]
+    s = _arr(solid, np.uint8)
+    st = L.les_format_field_vtk(C.byref(mesh), int(step), *[x.ctypes.data_as(_dp) for x in a],
+                                s.ctypes.data_as(_u8), str(path).encode())
+    if st != OK:
+        raise LesError(st, "format_field_vtk")
+
+
+def format_stats_vtk(mesh, mean4, stress6, path, lib=None):
+    L = lib or load()
+    m4 = [_arr(x) for x in mean4]
+    s6 = [_arr(x) for x in stress6]
+    st = L.les_format_stats_vtk(C.byref(mesh), _ptr_array(m4), _ptr_array(s6), str(path).encode())
+    if st != OK:
+        raise LesError(st, "format_stats_vtk")
+
+
+def write_checkpoint_files(mesh, f, solid, time_simulated, dt, next_step, d, unew3=None, lib=None):
+    L = lib or load()
+    a = [_arr(f[k]) for k in ("u", "v", "w", "p", "nu_t")]
+    s = _arr(solid, np.uint8)
+    u3 = [_arr(x) for x in unew3] if unew3 is not None else None
+    st = L.les_write_checkpoint_files(C.byref(mesh), _ptr_array(a), s.ctypes.data_as(_u8), C.c_double(time_simulated),
+                                      C.c_double(dt), int(next_step), str(d).encode(),
+                                      _ptr_array(u3) if u3 is not None else None)
+    if st != OK:
+        raise LesError(st, "write_checkpoint_files")
+
+
+def read_checkpoint_files(mesh, d, with_unew=False, lib=None):
+    L = lib or load()
+    n = mesh.n
+    a = [np.empty(n) for _ in range(5)]
+    s = np.empty(n, np.uint8)
+    u3 = [np.empty(n) for _ in range(3)] if with_unew else None
+    t, dt, step = C.c_double(), C.c_double(), C.c_int()
+    st = L.les_read_checkpoint_files(C.byref(mesh), str(d).encode(), _ptr_array(a), s.ctypes.data_as(_u8), C.byref(t),
+                                     C.byref(dt), C.byref(step), _ptr_array(u3) if u3 is not None else None)
+    if st != OK:
+        raise LesError(st, "read_checkpoint_files")
+    f = dict(zip(("u", "v", "w", "p", "nu_t"), a))
+    return step.value, t.value, dt.value, f, s, u3

@@ -724,3 +724,47 @@ int lo_step(const lo_mesh* m, lo_field* f, const lo_stencil* A, const lo_stencil
     if (dt_out) *dt_out = dt;
     return iters;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Statistics, src/statistics.cpp                                           */
+/* ------------------------------------------------------------------------ */
+
+/* src/statistics.cpp:110-130 */
+void lo_stats_update(int64_t n, const double* u, const double* v, const double* w, const double* p,
+                     double* const* s)
+{
+#pragma omp parallel for
+    for (int64_t i = 0; i < n; ++i) {
+        const double a = u[i], b = v[i], c = w[i], d = p[i];
+        s[0][i] += a;
+        s[1][i] += b;
+        s[2][i] += c;
+        s[3][i] += d;
+        s[4][i] += a * a;
+        s[5][i] += b * b;
+        s[6][i] += c * c;
+        s[7][i] += a * b;
+        s[8][i] += a * c;
+        s[9][i] += b * c;
+    }
+}
+
+/* src/statistics.cpp:143-184 */
+void lo_stats_finalize(int64_t n, int samples, const double* const* s, double* const* o)
+{
+    const double n_inv = 1.0 / (double)samples;
+#pragma omp parallel for
+    for (int64_t i = 0; i < n; ++i) {
+        const double um = s[0][i] * n_inv, vm = s[1][i] * n_inv, wm = s[2][i] * n_inv;
+        o[0][i] = um;
+        o[1][i] = vm;
+        o[2][i] = wm;
+        o[3][i] = s[3][i] * n_inv;
+        o[4][i] = (s[4][i] * n_inv) - (um * um);
+        o[5][i] = (s[5][i] * n_inv) - (vm * vm);
+        o[6][i] = (s[6][i] * n_inv) - (wm * wm);
+        o[7][i] = (s[7][i] * n_inv) - (um * vm);
+        o[8][i] = (s[8][i] * n_inv) - (um * wm);
+        o[9][i] = (s[9][i] * n_inv) - (vm * wm);
+    }
+}

@@ -112,6 +112,13 @@ typedef struct {
 int    lo_step(const lo_mesh* m, lo_field* f, const lo_stencil* A, const lo_stencil* L,
                const lo_step_params* prm, double* b_work, double* pcg_work, double* dt_out);
 
+/* src/statistics.cpp:98-131: sums[10] = u, v, w, p, uu, vv, ww, uv, uw, vw */
+void   lo_stats_update(int64_t n, const double* u, const double* v, const double* w, const double* p,
+                       double* const* sums);
+/* src/statistics.cpp:133-186 (without the file): out[10] = means of u, v, w,
+ * p and the stresses uu, vv, ww, uv, uw, vw */
+void   lo_stats_finalize(int64_t n, int samples, const double* const* sums, double* const* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -120,6 +120,17 @@ class Oracle:
     def threads(self):
         return self.lib.lo_get_threads()
 
+    # --- statistics (src/statistics.cpp)
+    def stats_update(self, u, v, w, p, sums):
+        arr = (_dp * 10)(*[_p(s) for s in sums])
+        self.lib.lo_stats_update(C.c_int64(u.size), _p(u), _p(v), _p(w), _p(p), arr)
+
+    def stats_finalize(self, samples, sums):
+        out = [np.empty_like(sums[0]) for _ in range(10)]
+        self.lib.lo_stats_finalize(C.c_int64(sums[0].size), C.c_int(samples), (_dp * 10)(*[_p(s) for s in sums]),
+                                   (_dp * 10)(*[_p(o) for o in out]))
+        return out
+
     # --- BLAS-1
     def dot(self, a, b):
         return self.lib.lo_dot(C.c_int64(a.size), _p(a), _p(b))

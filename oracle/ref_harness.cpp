@@ -15,11 +15,15 @@
 // IC-with-A preconditioner into solve_pressure_pcg (:362-363, :395-396).
 #include <cstdint>
 #include <cstring>
+#include <string>
 #include <vector>
 #include <omp.h>
+#include <unistd.h>
 
 #include "field.h"
+#include "io.h"
 #include "pressure.h"
+#include "statistics.h"
 
 // Defined in the reference's src/main.cpp (prototypes at src/main.cpp:20-29).
 double compute_adaptive_dt(const Field& field, const Mesh& mesh, double nu);
@@ -419,6 +423,82 @@ int ref_step(MESH_ARGS, double* u, double* v, double* w, double* un, double* vn,
     get(p, f.p, n); get(p_rhs, f.p_rhs, n); get(nu_t, f.nu_t, n);
     if (dt_out) *dt_out = dt;
     return it;
+}
+
+// ---- statistics and I/O (src/statistics.cpp, src/io.cpp) --------------------
+// The reference writes into paths relative to the working directory
+// (output/, checkpoint/); these wrappers run it inside `dir` and come back.
+namespace {
+struct InDir {
+    std::string old;
+    explicit InDir(const char* dir)
+    {
+        char buf[4096];
+        if (getcwd(buf, sizeof buf)) old = buf;
+        if (chdir(dir) != 0) old.clear();
+    }
+    ~InDir()
+    {
+        if (!old.empty() && chdir(old.c_str()) != 0) {}
+    }
+};
+}  // namespace
+
+// Runs init_statistics(start_step), then update_statistics for steps
+// 0..nsteps-1 with fields (u, v, w, p) of each step, copies out the ten sums
+// (u, v, w, p, uu, vv, ww, uv, uw, vw) and the sample count, and writes the
+// final statistics file with finalize_and_save(dir/filename).
+int ref_statistics(MESH_ARGS, int nsteps, int start_step, const double* const* uvwp, double* const* sums,
+                   const char* dir, const char* filename)
+{
+    Mesh m = MESH;
+    const size_t n = ncell(m);
+    Statistics st;
+    init_statistics(st, m, start_step);
+    Field f;
+    f.u.resize(n); f.v.resize(n); f.w.resize(n); f.p.resize(n);
+    for (int s = 0; s < nsteps; ++s) {
+        put(f.u, uvwp[4 * s + 0], n); put(f.v, uvwp[4 * s + 1], n);
+        put(f.w, uvwp[4 * s + 2], n); put(f.p, uvwp[4 * s + 3], n);
+        update_statistics(st, f, s);
+    }
+    const std::vector<double>* src[10] = {&st.sum_field.u, &st.sum_field.v, &st.sum_field.w, &st.sum_field.p,
+                                          &st.uu_sum, &st.vv_sum, &st.ww_sum, &st.uv_sum, &st.uw_sum, &st.vw_sum};
+    for (int q = 0; q < 10; ++q) get(sums[q], *src[q], n);
+    {
+        InDir d(dir);
+        finalize_and_save(st, m, filename);
+    }
+    return st.num_samples;
+}
+
+// write_field_vtk into dir/output/output_<step>.vtk
+void ref_write_field_vtk(MESH_ARGS, const double* u, const double* v, const double* w, const double* p,
+                         const double* nu_t, const uint8_t* solid, int step, const char* dir)
+{
+    Mesh m = MESH;
+    const size_t n = ncell(m);
+    Field f;
+    f.u.resize(n); f.v.resize(n); f.w.resize(n); f.p.resize(n); f.nu_t.resize(n); f.is_solid.assign(n, false);
+    put(f.u, u, n); put(f.v, v, n); put(f.w, w, n); put(f.p, p, n); put(f.nu_t, nu_t, n);
+    put_mask(f, solid, n);
+    InDir d(dir);
+    write_field_vtk(f, m, step);
+}
+
+// save_state into dir/checkpoint/checkpoint.{meta,data}
+void ref_save_state(MESH_ARGS, const double* u, const double* v, const double* w, const double* p,
+                    const double* nu_t, const uint8_t* solid, double time_simulated, double dt, int next_step,
+                    const char* dir)
+{
+    Mesh m = MESH;
+    const size_t n = ncell(m);
+    Field f;
+    f.u.resize(n); f.v.resize(n); f.w.resize(n); f.p.resize(n); f.nu_t.resize(n); f.is_solid.assign(n, false);
+    put(f.u, u, n); put(f.v, v, n); put(f.w, w, n); put(f.p, p, n); put(f.nu_t, nu_t, n);
+    put_mask(f, solid, n);
+    InDir d(dir);
+    save_state(f, m, time_simulated, dt, next_step);
 }
 
 }  // extern "C"

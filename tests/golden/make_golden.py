@@ -186,12 +186,67 @@ def run(name, shape, h, recipe, seed, ref):
           "traj iters", [list(d["traj%d_iters" % s]) for s in range(6)])
 
 
+def run_io(ref):
+    """Statistics (src/statistics.cpp) and file formats (src/io.cpp) on a
+    7x5x3 grid: three sampled steps with start_step 0 (the reference skips
+    step 0), the ten sums, the statistics file, one field file and one
+    checkpoint, stored as bytes."""
+    import ctypes as C
+    import tempfile
+    shape, h = (7, 5, 3), (0.125, 0.2, 1.0 / 3)
+    m = O.Mesh(*shape, *h)
+    n = m.n
+    rng = np.random.default_rng(77)
+    steps = [[rng.standard_normal(n) * s for s in (1.0, 0.3, 0.2, 2.0)] for _ in range(3)]
+    sums = [np.zeros(n) for _ in range(10)]
+    keep = [a for st in steps for a in st]
+    arr = (C.POINTER(C.c_double) * 12)(*[O._p(a) for a in keep])
+    outs = (C.POINTER(C.c_double) * 10)(*[O._p(a) for a in sums])
+    d = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        os.makedirs(os.path.join(tmp, "output"))
+        os.makedirs(os.path.join(tmp, "checkpoint"))
+        ns = ref.lib.ref_statistics(*ref._m(m), 3, 0, arr, outs, tmp.encode(), b"stats.vtk")
+        d["stats_samples"] = np.array([ns])
+        for s, st in enumerate(steps):
+            for k, a in zip(("u", "v", "w", "p"), st):
+                d["stats_in%d_%s" % (s, k)] = a
+        for q, k in enumerate(("u", "v", "w", "p", "uu", "vv", "ww", "uv", "uw", "vw")):
+            d["stats_sum_" + k] = sums[q]
+        d["stats_vtk"] = np.frombuffer(open(os.path.join(tmp, "stats.vtk"), "rb").read(), np.uint8)
+        f = {k: rng.standard_normal(n) for k in ("u", "v", "w", "p")}
+        f["nu_t"] = np.abs(rng.standard_normal(n)) * 1e-3
+        f["u"][3] = 1.0 / 3.0          # a few values that exercise %g rounding and exponents
+        f["v"][4] = -2.5e-7
+        f["p"][5] = 123456789.0
+        solid = (rng.random(n) < 0.3).astype(np.uint8)
+        for k, v in f.items():
+            d["io_" + k] = v
+        d["io_solid"] = solid
+        ref.lib.ref_write_field_vtk(*ref._m(m), *[O._p(f[k]) for k in ("u", "v", "w", "p", "nu_t")],
+                                    solid.ctypes.data_as(C.POINTER(C.c_uint8)), C.c_int(42), tmp.encode())
+        d["io_vtk_step"] = np.array([42])
+        d["io_vtk"] = np.frombuffer(open(os.path.join(tmp, "output", "output_42.vtk"), "rb").read(), np.uint8)
+        t_sim, dt, nxt = 0.0123456789012345678, 1e-4 / 3.0, 17
+        ref.lib.ref_save_state(*ref._m(m), *[O._p(f[k]) for k in ("u", "v", "w", "p", "nu_t")],
+                               solid.ctypes.data_as(C.POINTER(C.c_uint8)), C.c_double(t_sim), C.c_double(dt),
+                               C.c_int(nxt), tmp.encode())
+        d["ckpt_args"] = np.array([t_sim, dt, nxt])
+        d["ckpt_meta"] = np.frombuffer(open(os.path.join(tmp, "checkpoint", "checkpoint.meta"), "rb").read(), np.uint8)
+        d["ckpt_data"] = np.frombuffer(open(os.path.join(tmp, "checkpoint", "checkpoint.data"), "rb").read(), np.uint8)
+    d["mesh"] = np.array([*shape, *h])
+    np.savez_compressed(os.path.join(OUT, "io_tiny7.npz"), **d)
+    print("io_tiny7: samples", ns, "stats file", d["stats_vtk"].size, "B, field file", d["io_vtk"].size,
+          "B, checkpoint", d["ckpt_meta"].size, "+", d["ckpt_data"].size, "B")
+
+
 def main():
     O.build_ref()
     ref = O.Ref()
     ref.set_threads(1)
     for g in GRIDS:
         run(*g, ref)
+    run_io(ref)
 
 
 if __name__ == "__main__":
