@@ -92,10 +92,12 @@ __global__ void k_x_add(Geo g, double* __restrict__ x, const float* __restrict__
     x[id] = __dadd_rn(x[id], (double)e[id]);
 }
 
-// Inner state init: tolerance relative to the current outer residual.
+// Inner state init: tolerance relative to the current outer residual, but no
+// tighter than the outer tolerance needs (a third of it, for the FP32 rounding
+// of the correction): the last correction is not over-solved.
 __global__ void k_inner_init(SolverState* in, const SolverState* out, double inner_rtol, int max_iter)
 {
-    in->tol = inner_rtol * out->err;
+    in->tol = fmax(inner_rtol * out->err, out->tol / 3.0);
     in->max_iter = max_iter;
     in->k = 0;
     in->done = 0;
