@@ -204,6 +204,34 @@ __global__ void __launch_bounds__(CT, TJ == 8 ? 4 : 2) k_col_a(Geo g, ColMap m, 
 }
 
 // ---- pass B -----------------------------------------------------------------
+// Grid sums of ||r'||^2 and r'.z; the last block updates the inner state:
+// the first pass sets rho, later ones the convergence test, beta and rho.
+template <bool FIRST>
+__device__ __forceinline__ void pass_b_finish(const Acc& arr, const Acc& arz, double* partials, unsigned* counter,
+                                              double* sm, SolverState* st, SolverState* outer, int total_cap)
+{
+    double v[2] = {acc_value(arr), acc_value(arz)};
+    if (last_block_sum<2>(v, partials, counter, sm)) {
+        if (threadIdx.x == 0) {
+            if (FIRST) {
+                st->rho = v[1];
+            } else {
+                const double err = sqrt(v[0]);
+                const int kk = st->k + 1;
+                st->k = kk;
+                st->err = err;
+                const int total = outer->iters + 1;
+                outer->iters = total;
+                if (err < st->tol) { st->done = 1; st->status = LES_OK; }
+                else if (!isfinite(err)) { st->done = 1; st->status = LES_NONFINITE; }
+                else if (kk >= st->max_iter || total >= total_cap) { st->done = 1; st->status = LES_NOT_CONVERGED; }
+                st->beta = v[1] / st->rho;
+                st->rho = v[1];
+            }
+        }
+    }
+}
+
 template <int S, int TJ, bool FIRST>
 __global__ void __launch_bounds__(CT, (TJ == 4 && S <= 3) ? 3 : 2) k_col_b(Geo g, ColMap m, Coef k, ChebF cf, float inv_c0,
                                                const float* __restrict__ r_in, float* __restrict__ r_out,
@@ -344,26 +372,7 @@ __global__ void __launch_bounds__(CT, (TJ == 4 && S <= 3) ? 3 : 2) k_col_b(Geo g
                 }
         }
     }
-    double v[2] = {acc_value(arr), acc_value(arz)};
-    if (last_block_sum<2>(v, partials, counter, sm)) {
-        if (threadIdx.x == 0) {
-            if (FIRST) {
-                st->rho = v[1];
-            } else {
-                const double err = sqrt(v[0]);
-                const int kk = st->k + 1;
-                st->k = kk;
-                st->err = err;
-                const int total = outer->iters + 1;
-                outer->iters = total;
-                if (err < st->tol) { st->done = 1; st->status = LES_OK; }
-                else if (!isfinite(err)) { st->done = 1; st->status = LES_NONFINITE; }
-                else if (kk >= st->max_iter || total >= total_cap) { st->done = 1; st->status = LES_NOT_CONVERGED; }
-                st->beta = v[1] / st->rho;
-                st->rho = v[1];
-            }
-        }
-    }
+    pass_b_finish<FIRST>(arr, arz, partials, counter, sm, st, outer, total_cap);
 }
 
 // x += e + alpha p_last (FP64 solution, FP32 correction)
