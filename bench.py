@@ -391,6 +391,14 @@ def run_adjoint(args):
         t0 = time.perf_counter()
         g, gcs = c.adjoint_backward()
         t_bwd = time.perf_counter() - t0
+        # FP64 tangent-linear model along a seeded direction: the dot-product test
+        rng_t = np.random.default_rng(args.seed + 1)
+        d_in, d_cs = rng_t.standard_normal(g.size), 0.01
+        t0 = time.perf_counter()
+        dJ_tl = c.adjoint_tangent(d_in, d_cs)
+        t_tl = time.perf_counter() - t0
+        proj = float(np.dot(g, d_in) + gcs * d_cs)
+        tl_err = abs(dJ_tl - proj) / max(abs(proj), 1e-300)
     rng = np.random.default_rng(args.seed)
     ny, nz = shape[1], shape[2]
     cand = [(j, k) for j in range(1, ny - 1) for k in range(1, nz - 1)]
@@ -416,7 +424,8 @@ def run_adjoint(args):
                        "fd_step": hs, "fd_entries": 16},
             "J": J, "grad_cs": gcs, "fd_cs": fdc, "cs_rel_err": cs_err, "grad_inlet_max_abs": float(np.abs(g).max()),
             "median_rel_err": float(np.median(errs)), "entries": rows,
-            "forward_s": t_fwd, "backward_s": t_bwd, "backward_over_forward": t_bwd / t_fwd}
+            "forward_s": t_fwd, "backward_s": t_bwd, "backward_over_forward": t_bwd / t_fwd,
+            "tangent": {"dJ": dJ_tl, "adjoint_projection": proj, "rel_err": tl_err, "seconds": t_tl}}
     print(json.dumps(line), flush=True)
     return 0
 

@@ -307,6 +307,12 @@ les_status les_adjoint_forward(les_ctx* ctx, const les_adjoint_params* prm, doub
 /* grad_inlet: ny*nz values (dJ/du_in), grad_cs: dJ/dCs.  Leaves the fields
  * at the first checkpoint's recomputation (restore them to continue). */
 les_status les_adjoint_backward(les_ctx* ctx, double* grad_inlet, double* grad_cs);
+/* Tangent-linear model (FP64): the directional derivative dJ along
+ * (d_inlet, d_cs) by forward differentiation of the same steps from the first
+ * checkpoint; with the backward's gradient g it must satisfy
+ * dJ = g . d_inlet + grad_cs * d_cs (the dot-product test).  d_inlet may be
+ * NULL.  Leaves the fields at step N. */
+les_status les_adjoint_tangent(les_ctx* ctx, const double* d_inlet, double d_cs, double* dJ);
 
 /* ---- autotuner (no reference counterpart) ------------------------------- */
 /* Times the fused inner passes of the mixed-precision PCG for opts on the

@@ -393,6 +393,157 @@ les_status objective(les_ctx* c, AdjWork& a, int add_adjoint)
     return check_launch(c, "objective");
 }
 
+// ---- tangent-linear model: the forward derivative of the same step ------------
+// du_in (ny*nz) / dcs are the direction; dU the tangent of the velocity.
+
+// dnu = K dS + dK/dCs S dcs at interior fluid cells (0 where the nu_t
+// boundary values overwrite it)
+__global__ void k_tl_sgs(Geo g, Dx d, double K, double dK_dCs, double dcs, const uint8_t* __restrict__ solid,
+                         const double* __restrict__ u, const double* __restrict__ v, const double* __restrict__ w,
+                         const double* __restrict__ du, const double* __restrict__ dv, const double* __restrict__ dw,
+                         double* __restrict__ dnu)
+{
+    int i, j, k;
+    if (!coords(g, i, j, k)) return;
+    const int id = i * g.si + j * g.sj + k;
+    double r = 0.0;
+    if (interior(g, i, j, k) && !solid[id]) {
+        const int si = g.si, sj = g.sj;
+        auto gx = [&](const double* f) { return (f[id + si] - f[id - si]) * d.i2dx; };
+        auto gy = [&](const double* f) { return (f[id + sj] - f[id - sj]) * d.i2dy; };
+        auto gz = [&](const double* f) { return (f[id + 1] - f[id - 1]) * d.i2dz; };
+        const double Sxx = gx(u), Syy = gy(v), Szz = gz(w);
+        const double Sxy = 0.5 * (gy(u) + gx(v)), Sxz = 0.5 * (gz(u) + gx(w)), Syz = 0.5 * (gz(v) + gy(w));
+        const double S = sqrt(2.0 * (Sxx * Sxx + Syy * Syy + Szz * Szz) + 4.0 * (Sxy * Sxy + Sxz * Sxz + Syz * Syz));
+        const double dSxx = gx(du), dSyy = gy(dv), dSzz = gz(dw);
+        const double dSxy = 0.5 * (gy(du) + gx(dv)), dSxz = 0.5 * (gz(du) + gx(dw)), dSyz = 0.5 * (gz(dv) + gy(dw));
+        const double dS = S > 0.0 ? (2.0 * (Sxx * dSxx + Syy * dSyy + Szz * dSzz) +
+                                     4.0 * (Sxy * dSxy + Sxz * dSxz + Syz * dSyz)) / S
+                                  : 0.0;
+        r = K * dS + dK_dCs * S * dcs;
+    }
+    dnu[id] = r;
+}
+
+// dX1 at interior cells: the derivative of o = f + dt(-(u.grad) f + (nu + nu_t) lap f)
+__global__ void k_tl_momentum(Geo g, Dx d, double dt, double nu, const double* __restrict__ u,
+                              const double* __restrict__ v, const double* __restrict__ w,
+                              const double* __restrict__ nu_t, const double* __restrict__ du,
+                              const double* __restrict__ dv, const double* __restrict__ dw,
+                              const double* __restrict__ dnu, double* __restrict__ ox, double* __restrict__ oy,
+                              double* __restrict__ oz)
+{
+    int i, j, k;
+    if (!coords(g, i, j, k)) return;
+    const int id = i * g.si + j * g.sj + k;
+    double* o3[3] = {ox, oy, oz};
+    if (!interior(g, i, j, k)) {
+        ox[id] = oy[id] = oz[id] = 0.0;   // overwritten by the boundary conditions
+        return;
+    }
+    const double* f3[3] = {u, v, w};
+    const double* d3[3] = {du, dv, dw};
+    const int si = g.si, sj = g.sj;
+    const double ne = nu + nu_t[id];
+    for (int q = 0; q < 3; ++q) {
+        const double* f = f3[q];
+        const double* df = d3[q];
+        auto grad = [&](const double* a, double& gxv, double& gyv, double& gzv, double& lap) {
+            const double c = a[id];
+            gxv = (a[id + si] - a[id - si]) * d.i2dx;
+            gyv = (a[id + sj] - a[id - sj]) * d.i2dy;
+            gzv = (a[id + 1] - a[id - 1]) * d.i2dz;
+            lap = (a[id + si] - 2 * c + a[id - si]) * d.idx2 + (a[id + sj] - 2 * c + a[id - sj]) * d.idy2 +
+                  (a[id + 1] - 2 * c + a[id - 1]) * d.idz2;
+        };
+        double fx, fy, fz, fl, gx, gy, gz, gl;
+        grad(f, fx, fy, fz, fl);
+        grad(df, gx, gy, gz, gl);
+        const double dadv = du[id] * fx + dv[id] * fy + dw[id] * fz + u[id] * gx + v[id] * gy + w[id] * gz;
+        o3[q][id] = df[id] + dt * (-dadv + dnu[id] * fl + ne * gl);
+    }
+}
+
+// the linearised velocity boundary conditions: the inlet takes the direction
+// of the profile, walls and solids 0, the outlet copies plane nx-2
+// (faces; the interior solids follow in k_tl_solids, after the outlet copy)
+__global__ void k_tl_bc(Geo g, const uint8_t* __restrict__ solid, double* u, double* v, double* w,
+                        const double* __restrict__ din)
+{
+    int i, j, k;
+    if (!coords(g, i, j, k)) return;
+    const bool jk_in = j >= 1 && j <= g.ny - 2 && k >= 1 && k <= g.nz - 2;
+    if (jk_in && i > 0 && i < g.nx - 1) return;
+    const int id = i * g.si + j * g.sj + k;
+    if (!jk_in) { u[id] = v[id] = w[id] = 0.0; return; }
+    if (i == 0) {
+        if (!solid[id]) { u[id] = din ? din[j * g.nz + k] : 0.0; v[id] = 0.0; w[id] = 0.0; }
+        return;
+    }
+    const int src = id - g.si;
+    u[id] = u[src]; v[id] = v[src]; w[id] = w[src];
+}
+
+__global__ void k_tl_solids(Geo g, const uint8_t* __restrict__ solid, double* u, double* v, double* w)
+{
+    int i, j, k;
+    if (!coords(g, i, j, k)) return;
+    if (!interior(g, i, j, k)) return;
+    const int id = i * g.si + j * g.sj + k;
+    if (solid[id]) u[id] = v[id] = w[id] = 0.0;
+}
+
+// db = -(rho/dt) D dU (masked like build_b)
+__global__ void k_tl_div(Geo g, Dx d, double m_rho_dt, const uint8_t* __restrict__ solid, const double* __restrict__ u,
+                         const double* __restrict__ v, const double* __restrict__ w, double* __restrict__ db)
+{
+    int i, j, k;
+    if (!coords(g, i, j, k)) return;
+    const int id = i * g.si + j * g.sj + k;
+    if (solid[id] || i == g.nx - 1) { db[id] = 0.0; return; }
+    double a, b, c;
+    if (i == 0) a = (u[id + g.si] - u[id]) * d.idx;
+    else a = (u[id + g.si] - u[id - g.si]) * d.i2dx;
+    if (j == 0) b = (v[id + g.sj] - v[id]) * d.idy;
+    else if (j == g.ny - 1) b = (v[id] - v[id - g.sj]) * d.idy;
+    else b = (v[id + g.sj] - v[id - g.sj]) * d.i2dy;
+    if (k == 0) c = (w[id + 1] - w[id]) * d.idz;
+    else if (k == g.nz - 1) c = (w[id] - w[id - 1]) * d.idz;
+    else c = (w[id + 1] - w[id - 1]) * d.i2dz;
+    db[id] = m_rho_dt * (a + b + c);
+}
+
+// dX3 = dX2 - (dt/rho) G dp at interior cells
+__global__ void k_tl_correct(Geo g, Dx d, double dt_over_rho, const double* __restrict__ dp, double* u, double* v,
+                             double* w)
+{
+    int i, j, k;
+    if (!coords(g, i, j, k)) return;
+    if (!interior(g, i, j, k)) return;
+    const int id = i * g.si + j * g.sj + k;
+    u[id] -= dt_over_rho * ((dp[id + g.si] - dp[id - g.si]) * d.i2dx);
+    v[id] -= dt_over_rho * ((dp[id + g.sj] - dp[id - g.sj]) * d.i2dy);
+    w[id] -= dt_over_rho * ((dp[id + 1] - dp[id - 1]) * d.i2dz);
+}
+
+// acc[0] += scale * sum_box U . dU
+__global__ void k_tl_objective(Geo g, int i0, int i1, int j0, int j1, int k0, int k1, double scale,
+                               const double* __restrict__ u, const double* __restrict__ v, const double* __restrict__ w,
+                               const double* __restrict__ du, const double* __restrict__ dv,
+                               const double* __restrict__ dw, double* partials, unsigned* counter, double* acc)
+{
+    __shared__ double sm[32];
+    int i, j, k;
+    double e[1] = {0.0};
+    if (coords(g, i, j, k)) {
+        const int id = i * g.si + j * g.sj + k;
+        if (i >= i0 && i < i1 && j >= j0 && j < j1 && k >= k0 && k < k1)
+            e[0] = u[id] * du[id] + v[id] * dv[id] + w[id] * dw[id];
+    }
+    if (last_block_sum<1>(e, partials, counter, sm))
+        if (threadIdx.x == 0 && threadIdx.y == 0) acc[0] += scale * e[0];
+}
+
 // one forward step with the checks the gradient relies on
 les_status fwd_step(les_ctx* c, const les_step_params* prm)
 {
@@ -401,6 +552,35 @@ les_status fwd_step(les_ctx* c, const les_step_params* prm)
     if (st) return st;
     if (s.status != LES_OK) return fail(c, (les_status)s.status, "adjoint: a forward pressure solve did not converge");
     return LES_OK;
+}
+
+// sol = A^-1 rhs with the step's PCG to adj_rel_tol * ||rhs|| (sol holds the
+// warm start on entry)
+les_status solve_linear(les_ctx* c, AdjWork& a, double* rhs, double* sol, const char* what)
+{
+    double rr = 0.0;
+    les_status st = dot_dev(c, rhs, rhs, &rr);
+    if (st) return st;
+    if (!(rr > 0.0)) return zero(c, sol, c->g.n);
+    les_pcg_opts o = a.prm.step.pcg;
+    o.tol = a.prm.adj_rel_tol * std::sqrt(rr);
+    if (o.precision == LES_MIXED) {
+        // an inner FP32 CG that stagnates on this non-symmetric system ends
+        // after a bounded number of iterations; the FP64 outer correction
+        // carries on from what it reached
+        if (o.inner_max_iter <= 0) o.inner_max_iter = 400;
+        if (o.max_outer < 200) o.max_outer = 200;
+    }
+    double* sb = c->slot[LES_B];
+    double* sp = c->slot[LES_P];
+    c->slot[LES_B] = rhs;
+    c->slot[LES_P] = sol;
+    les_pcg_result r{};
+    st = o.precision == LES_MIXED ? pcg_mixed_impl(c, &o, &r, 0) : pcg_fp64(c, &o, &r, 0);
+    c->slot[LES_B] = sb;
+    c->slot[LES_P] = sp;
+    if (st == LES_NOT_CONVERGED) return fail(c, st, std::string(what) + ": a pressure solve did not converge");
+    return st;
 }
 
 // Reverses one step whose input velocity is in the velocity slots (a.lu holds
@@ -424,31 +604,7 @@ les_status step_adjoint(les_ctx* c, AdjWork& a)
     // p = A^-1 b: lb = A^-T lp = W A^-1 (W^-1 lp)
     launch(c, k_scale_w, gr, bl, g, a.lp, 1);
     if ((st = check_launch(c, "adjoint correction"))) return st;
-    double rr = 0.0;
-    if ((st = dot_dev(c, a.lp, a.lp, &rr))) return st;
-    if (rr > 0.0) {
-        les_pcg_opts o = p.pcg;
-        o.tol = a.prm.adj_rel_tol * std::sqrt(rr);
-        if (o.precision == LES_MIXED) {
-            // an inner FP32 CG that stagnates on this non-symmetric system
-            // ends after a bounded number of iterations; the FP64 outer
-            // correction carries on from what it reached
-            if (o.inner_max_iter <= 0) o.inner_max_iter = 400;
-            if (o.max_outer < 200) o.max_outer = 200;
-        }
-        double* sb = c->slot[LES_B];
-        double* sp = c->slot[LES_P];
-        c->slot[LES_B] = a.lp;
-        c->slot[LES_P] = a.lb;
-        les_pcg_result r{};
-        st = o.precision == LES_MIXED ? pcg_mixed_impl(c, &o, &r, 0) : pcg_fp64(c, &o, &r, 0);
-        c->slot[LES_B] = sb;
-        c->slot[LES_P] = sp;
-        if (st == LES_NOT_CONVERGED) return fail(c, st, "adjoint: the adjoint pressure solve did not converge");
-        if (st) return st;
-    } else if ((st = zero(c, a.lb, g.n))) {
-        return st;
-    }
+    if ((st = solve_linear(c, a, a.lp, a.lb, "adjoint"))) return st;
     // lb holds A^-1 W^-1 lp; the scaled copy goes to lp (lb stays the next warm start)
     if ((st = copy(c, a.lp, a.lb))) return st;
     launch(c, k_scale_w, gr, bl, g, a.lp, 0);
@@ -603,6 +759,76 @@ les_status les_adjoint_backward(les_ctx* c, double* grad_inlet, double* grad_cs)
     if (st) return st;
     if (grad_inlet) std::memcpy(grad_inlet, gi.data(), sizeof(double) * gi.size());
     if (grad_cs) *grad_cs = h[1];
+    return LES_OK;
+}
+
+les_status les_adjoint_tangent(les_ctx* c, const double* d_inlet, double d_cs, double* dJ)
+{
+    if (!c || !c->adj || !c->adj->forward_done) return c ? fail(c, LES_BAD_ARG, "tangent: run the forward first")
+                                                         : LES_BAD_ARG;
+    cudaSetDevice(c->device);
+    AdjWork& a = *c->adj;
+    const les_adjoint_params& prm = a.prm;
+    const les_step_params& p = prm.step;
+    const Geo& g = c->g;
+    const size_t n = a.n, nin = (size_t)g.ny * g.nz;
+    const Dx d = dx_of(c->mesh);
+    const dim3 gr = cell_grid(g), bl = cell_block();
+    les_status st;
+    // tangent work: dU (a.lx), intermediate (a.h[0..2]), dnu (a.lnu), db (a.lp), dp (a.lb), direction (a.h[3])
+    if ((st = zero(c, a.acc, 2)) || (st = zero(c, a.lb, n))) return st;
+    for (int q = 0; q < 3; ++q)
+        if ((st = zero(c, a.lx[q], n))) return st;
+    double* din = a.h[3];
+    if (d_inlet) {
+        st = check_cuda(c, cudaMemcpyAsync(din, d_inlet, sizeof(double) * nin, cudaMemcpyHostToDevice, c->stream),
+                        "tangent direction");
+        if (st) return st;
+    } else if ((st = zero(c, din, nin))) {
+        return st;
+    }
+    // U_0 = BC(initial fields): dU_0 is the profile direction on the inlet
+    const int sl[4] = {LES_U, LES_V, LES_W, LES_P};
+    for (int q = 0; q < 4; ++q)
+        if ((st = copy(c, c->slot[sl[q]], a.ck[q]))) return st;
+    launch(c, k_tl_bc, gr, bl, g, (const uint8_t*)c->mask, a.lx[0], a.lx[1], a.lx[2], (const double*)din);
+    launch(c, k_tl_solids, gr, bl, g, (const uint8_t*)c->mask, a.lx[0], a.lx[1], a.lx[2]);
+    const double delta = std::pow(c->mesh.dx * c->mesh.dy * c->mesh.dz, 1.0 / 3.0);
+    const double K = std::pow(p.cs * delta, 2);
+    for (int step = 0; step < prm.steps; ++step) {
+        if ((st = sgs_nut_dev(c, p.cs, 0))) return st;
+        launch(c, k_tl_sgs, gr, bl, g, d, K, 2.0 * p.cs * delta * delta, d_cs, (const uint8_t*)c->mask,
+               (const double*)c->slot[LES_U], (const double*)c->slot[LES_V], (const double*)c->slot[LES_W],
+               (const double*)a.lx[0], (const double*)a.lx[1], (const double*)a.lx[2], a.lnu);
+        launch(c, k_tl_momentum, gr, bl, g, d, p.dt_fixed, p.nu, (const double*)c->slot[LES_U],
+               (const double*)c->slot[LES_V], (const double*)c->slot[LES_W], (const double*)c->slot[LES_NU_T],
+               (const double*)a.lx[0], (const double*)a.lx[1], (const double*)a.lx[2], (const double*)a.lnu, a.h[0],
+               a.h[1], a.h[2]);
+        launch(c, k_tl_bc, gr, bl, g, (const uint8_t*)c->mask, a.h[0], a.h[1], a.h[2], (const double*)din);
+        launch(c, k_tl_solids, gr, bl, g, (const uint8_t*)c->mask, a.h[0], a.h[1], a.h[2]);
+        launch(c, k_tl_div, gr, bl, g, d, -p.rho / p.dt_fixed, (const uint8_t*)c->mask, (const double*)a.lx[0],
+               (const double*)a.lx[1], (const double*)a.lx[2], a.lp);
+        if ((st = check_launch(c, "tangent step"))) return st;
+        if ((st = solve_linear(c, a, a.lp, a.lb, "tangent"))) return st;
+        launch(c, k_tl_correct, gr, bl, g, d, p.dt_fixed / p.rho, (const double*)a.lb, a.h[0], a.h[1], a.h[2]);
+        launch(c, k_tl_bc, gr, bl, g, (const uint8_t*)c->mask, a.h[0], a.h[1], a.h[2], (const double*)din);
+        launch(c, k_tl_solids, gr, bl, g, (const uint8_t*)c->mask, a.h[0], a.h[1], a.h[2]);
+        for (int q = 0; q < 3; ++q)
+            if ((st = copy(c, a.lx[q], a.h[q]))) return st;
+        // the forward step itself (from the same U_n), then the J term of U_{n+1}
+        if ((st = fwd_step(c, &p))) return st;
+        const int* b = prm.box;
+        launch(c, k_tl_objective, gr, bl, g, b[0], b[1], b[2], b[3], b[4], b[5], 1.0 / prm.steps,
+               (const double*)c->slot[LES_U], (const double*)c->slot[LES_V], (const double*)c->slot[LES_W],
+               (const double*)a.lx[0], (const double*)a.lx[1], (const double*)a.lx[2], c->partials, c->counters + 18,
+               a.acc);
+        if ((st = check_launch(c, "tangent objective"))) return st;
+    }
+    double h[2];
+    st = check_cuda(c, cudaMemcpyAsync(h, a.acc, sizeof h, cudaMemcpyDeviceToHost, c->stream), "read dJ");
+    if (!st) st = check_cuda(c, cudaStreamSynchronize(c->stream), "read dJ");
+    if (st) return st;
+    if (dJ) *dJ = h[0];
     return LES_OK;
 }
 

@@ -583,3 +583,15 @@ def read_checkpoint_files(mesh, d, with_unew=False, lib=None):
         raise LesError(st, "read_checkpoint_files")
     f = dict(zip(("u", "v", "w", "p", "nu_t"), a))
     return step.value, t.value, dt.value, f, s, u3
+
+
+def _ctx_adjoint_tangent(self, d_inlet, d_cs):
+    dJ = C.c_double()
+    self.lib.les_adjoint_tangent.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.POINTER(C.c_double)]
+    a = None if d_inlet is None else _arr(d_inlet)
+    self._chk(self.lib.les_adjoint_tangent(self.h, None if a is None else a.ctypes.data, C.c_double(d_cs),
+                                           C.byref(dJ)))
+    return dJ.value
+
+
+Context.adjoint_tangent = _ctx_adjoint_tangent

@@ -86,3 +86,20 @@ def test_adjoint_is_independent_of_the_checkpoint_interval():
     assert J1 == J4 == J6
     assert np.array_equal(g1, g4) and np.array_equal(g4, g6)
     assert c1 == c4 == c6
+
+
+def test_tangent_linear_dot_product_test():
+    """The FP64 tangent-linear model and the adjoint are exact linearisations
+    of the same discrete map: dJ along a random direction equals the
+    adjoint gradient projected on it (to the pressure-solve tolerance)."""
+    prof, cs = _profile(), 0.17
+    rng = np.random.default_rng(31)
+    d_in = rng.standard_normal(prof.size)
+    d_cs = 0.3
+    with G.Context(G.Mesh(*SHAPE, H, H, H)) as c:
+        lmax = _setup(c, prof)
+        c.adjoint_forward(_params(lmax, cs), STEPS, 4, BOX)
+        g, gcs = c.adjoint_backward()
+        dJ = c.adjoint_tangent(d_in, d_cs)
+    proj = float(np.dot(g, d_in) + gcs * d_cs)
+    assert abs(dJ - proj) <= 1e-8 * abs(proj), (dJ, proj)
