@@ -75,6 +75,28 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(x, pg, device="cpu"):
+    """The slowest rank's value of x, on every rank (x itself without a group)."""
+    if not pg:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def shard_cases(sizes, rank, world):
+    """Independent cases over ranks with no exchange: longest first onto the
+    least-loaded rank (by cell count).  Returns this rank's case indices."""
+    load = [0] * world
+    owner = [0] * len(sizes)
+    for i in sorted(range(len(sizes)), key=lambda q: (-sizes[q], q)):
+        r = min(range(world), key=lambda q: (load[q], q))
+        owner[i] = r
+        load[r] += sizes[i]
+    return [i for i in range(len(sizes)) if owner[i] == rank]
+
+
 def dist_env():
     return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
             int(os.environ.get("LOCAL_RANK", 0)))
@@ -271,10 +293,15 @@ def run_batch(args):
     import les_gb300 as G
 
     rank, world, local = dist_env()
-    if rank != 0:
-        return 0
-    torch.cuda.set_device(0)
-    specs = les_cases.batch_cases(args.batch, args.seed)
+    torch.cuda.set_device(local if world > 1 else 0)
+    pg = None
+    if world > 1:   # the cases are independent: each rank advances its share, no exchange
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        pg = dist
+    all_specs = les_cases.batch_cases(args.batch, args.seed)
+    cells_all = sum(int(np.prod(s["shape"])) for s in all_specs)
+    specs = [all_specs[i] for i in shard_cases([int(np.prod(s["shape"])) for s in all_specs], rank, world)]
     meshes = [G.Mesh(*s["shape"], s["h"], s["h"], s["h"]) for s in specs]
     ens = G.Ensemble(meshes)
     prm = []
@@ -304,7 +331,9 @@ def run_batch(args):
     ens.sync()
     warm_s = time.perf_counter() - t0
     launches0 = sum(c.launch_count() for c in ens.cases)
-    clocks = Clocks(0)
+    clocks = Clocks(local if world > 1 else 0)
+    if pg:
+        pg.barrier()
     clocks.start()
     iters, worst = [], 0.0
     t0 = time.perf_counter()
@@ -315,24 +344,31 @@ def run_batch(args):
         bad = [x.status for x in st if x.status != G.OK]
         if bad:
             raise RuntimeError("ensemble step: %d cases did not converge" % len(bad))
-    wall = time.perf_counter() - t0
+    wall = max_over_ranks(time.perf_counter() - t0, pg, "cuda" if torch.cuda.is_available() else "cpu")
     clk = clocks.stop()
     launches = sum(c.launch_count() for c in ens.cases) - launches0
-    value = cells * args.steps / wall / 1e6
+    value = cells_all * args.steps / wall / 1e6   # every rank's cases over the slowest rank's time
+    ens.close()
+    if pg:
+        pg.barrier()
+        pg.destroy_process_group()
+    if rank != 0:
+        return 0
     line = {"metric": "Mcell-steps/s, ensemble of %d ragged cases, mixed FP32/FP64 at div<=1e-8" % args.batch,
-            "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 inner / f64 outer", "data": "synthetic",
             "config": {"workload": "batch: %d cases, dims from {32,48,64,80,96}, cube obstacle, Cs U[0.1,0.2], "
                                    "cheb(4)-PCG mixed, one graph launch per step" % args.batch,
-                       "cells": cells, "timing": "host wall clock around each step's launch + stats sync",
+                       "cells": cells_all, "cells_rank0": cells,
+                       "parallelism": "cases sharded over %d ranks, no exchange" % world if world > 1 else "single",
+                       "timing": "host wall clock around each step's launch + stats sync, max over ranks",
                        "l2": "inputs (~%.1f GB) larger than L2" % (cells * 120 / 1e9),
                        "autotune_us_per_iteration": tune_us, "autotune_s": tune_s,
                        "first_steps_with_capture_s": warm_s},
             "gpu_launches": launches, "iters_inner_mean": statistics.mean(iters), "rel_residual_max": worst,
             "clocks": clk}
     print(json.dumps(line), flush=True)
-    ens.close()
     return 0
 
 
@@ -519,11 +555,7 @@ def run_ours(args):
     ctx.sync()
     prof = ctx.profile_all()
     ctx.profile(0)
-    t_dev = sum(rec["ms"]) / 1e3
-    if pg:
-        t = torch.tensor([t_dev], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        t_dev = float(t.item())
+    t_dev = max_over_ranks(sum(rec["ms"]) / 1e3, pg, "cuda" if torch.cuda.is_available() else "cpu")
     value = world * n * args.steps / t_dev / 1e6
 
     # ---- end to end through the C ABI with pinned host buffers
