@@ -172,18 +172,20 @@ __global__ void __launch_bounds__(CT, TJ == 8 ? 4 : 2) k_col_a(Geo g, ColMap m, 
                 const float cc = ident ? 1.f : k.c0, cx = ident ? 0.f : k.x1;
                 const float ce = (ident || C == g.nx - 2) ? 0.f : k.x1;
                 const float cy = ident ? 0.f : k.y1, cz = ident ? 0.f : k.z1;
-                float sq = 0.f;
+                float sq = 0.f, qv[TJ + 1];
+                // all rows' products first (one basic block), then the owned stores
 #pragma unroll
                 for (int r = 1; r <= TJ; ++r) {
                     const float pc = p1[r];
                     const float pb = __shfl_up_sync(FULL, pc, 1);
                     const float pt = __shfl_down_sync(FULL, pc, 1);
-                    if ((s.own >> r) & 1u) {
-                        const float val = cc * pc + cx * p2[r] + ce * p0[r] + cy * (p1[r - 1] + p1[r + 1]) +
-                                          cz * (pb + pt);
-                        q[cb + r * g.sj] = val;
-                        sq = fmaf(pc, val, sq);
-                    }
+                    qv[r] = cc * pc + cx * p2[r] + ce * p0[r] + cy * (p1[r - 1] + p1[r + 1]) + cz * (pb + pt);
+                }
+#pragma unroll
+                for (int r = 1; r <= TJ; ++r) {
+                    const bool o = (s.own >> r) & 1u;
+                    if (o) q[cb + r * g.sj] = qv[r];
+                    sq = fmaf(o ? p1[r] : 0.f, qv[r], sq);
                 }
                 acc_add(acc, sq);
             }
@@ -253,6 +255,7 @@ __global__ void __launch_bounds__(CT, (TJ == 4 && S <= 3) ? 3 : 2) k_col_b(Geo g
         float zr[NL][3][H];      // z_L at planes I - L - d (L = 1 .. S-1 at [L-1])
         float pcr[NL][2][H];     // pc_L at planes I - L - d
         float vr[H], vq[H];      // r, q of the plane being fetched
+        float zS[H];             // the last level's z at its plane, before the stores
 #pragma unroll
         for (int d = 0; d <= S; ++d)
 #pragma unroll
@@ -291,22 +294,24 @@ __global__ void __launch_bounds__(CT, (TJ == 4 && S <= 3) ? 3 : 2) k_col_b(Geo g
                 const int base = I * g.si + s.j0 * g.sj + s.kl;
                 const float dinv = I == g.nx - 1 ? 1.f : inv_c0;   // Jacobi: identity row at the outlet
                 float srr = 0.f, srz = 0.f;
+                // the arithmetic of all rows first (one basic block), then
+                // the stores and sums of the owned cells
 #pragma unroll
-                for (int r = 0; r < H; ++r) {
-                    const float rv = FIRST ? vr[r] : fmaf(-alpha, vq[r], vr[r]);
-                    rp[0][r] = rv;
-                    if (pown && ((s.own >> r) & 1u)) {
+                for (int r = 0; r < H; ++r) rp[0][r] = FIRST ? vr[r] : fmaf(-alpha, vq[r], vr[r]);
+                if (pown) {
+#pragma unroll
+                    for (int r = S; r < S + TJ; ++r) {
+                        const float rv = rp[0][r];
+                        const bool o = (s.own >> r) & 1u;
                         const int id = base + r * g.sj;
-                        r_out[id] = rv;
-                        srr = fmaf(rv, rv, srr);
+                        if (o) r_out[id] = rv;
+                        srr = fmaf(o ? rv : 0.f, rv, srr);
                         if (S == 0) {
                             const float zv = rv * dinv;
-                            z_out[id] = zv;
-                            srz = fmaf(rv, zv, srz);
+                            if (o) z_out[id] = zv;
+                            srz = fmaf(o ? rv : 0.f, zv, srz);
                         }
                     }
-                }
-                if (pown) {
                     acc_add(arr, srr);
                     if (S == 0) acc_add(arz, srz);
                 }
@@ -350,12 +355,19 @@ __global__ void __launch_bounds__(CT, (TJ == 4 && S <= 3) ? 3 : 2) k_col_b(Geo g
                     if (LV < S) {
                         zr[LV - 1][0][r] = zk;
                         pcr[LV - 1][0][r] = pck;
-                    } else if (out_plane && ((s.own >> r) & 1u)) {
-                        z_out[pbase + r * g.sj] = zk;
-                        s2 = fmaf(rv, zk, s2);
+                    } else {
+                        zS[r] = zk;
                     }
                 }
-                if (out_plane) acc_add(arz, s2);
+                if (LV == S && out_plane) {   // stores and r'.z of the owned cells
+#pragma unroll
+                    for (int r = S; r < S + TJ; ++r) {
+                        const bool o = (s.own >> r) & 1u;
+                        if (o) z_out[pbase + r * g.sj] = zS[r];
+                        s2 = fmaf(o ? rp[S][r] : 0.f, zS[r], s2);
+                    }
+                    acc_add(arz, s2);
+                }
             }
             // ---- rotate the rings by one plane
 #pragma unroll
