@@ -59,7 +59,8 @@ def parse():
     ap.add_argument("--adj-steps", type=int, default=50, help="adjoint workload: forward steps")
     ap.add_argument("--fd-step", type=float, default=1e-6, help="adjoint workload: finite-difference step")
     ap.add_argument("--batch", type=int, default=64, help="cases of the batch workload")
-    ap.add_argument("--tune", type=int, default=1, help="batch workload: run the ensemble autotuner first")
+    ap.add_argument("--tune", type=int, default=1,
+                    help="run the strip-shape autotuner before warm-up (column passes, built-in rows/chunks)")
     ap.add_argument("--precond", default="cheb", choices=("cheb", "jacobi", "ic"))
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
@@ -71,6 +72,7 @@ def parse():
     ap.add_argument("--rows", default="0,0", help="rows per strip of the column passes A,B (0 = built-in)")
     ap.add_argument("--chunks", default="0,0", help="planes per march chunk of the column passes A,B (0 = auto)")
     ap.add_argument("--graph", type=int, default=1, help="replay each time step as one CUDA graph (LES_OPT_GRAPH)")
+    ap.add_argument("--pdl", type=int, default=1, help="column passes as programmatic dependent launches (LES_OPT_PDL)")
     ap.add_argument("--prof-steps", type=int, default=2, help="extra steps timed per kernel for the roofline")
     return ap.parse_args()
 
@@ -485,11 +487,15 @@ def run_ours(args):
     ctx.set_option(G.OPT_FUSED, args.fused)
     ctx.set_option(G.OPT_TMA, args.tma)
     ctx.set_option(G.OPT_GRAPH, args.graph)
+    ctx.set_option(G.OPT_PDL, args.pdl)
     ra, rb = (int(x) for x in args.rows.split(","))
     ca, cb = (int(x) for x in args.chunks.split(","))
     for opt, v in ((G.OPT_ROWS_A, ra), (G.OPT_ROWS_B, rb), (G.OPT_CHUNK_A, ca), (G.OPT_CHUNK_B, cb)):
         ctx.set_option(opt, v)
     prm = step_params(G, les_cases, args.precond, lmax, G.MIXED, args.inner_rtol)
+    tune_us = None   # strip rows and chunk lengths from the autotuner (outside the timed region)
+    if args.tune and args.fused == 1 and args.rows == "0,0" and args.chunks == "0,0" and args.precond != "ic":
+        tune_us = ctx.autotune(prm.pcg)
     ctx64 = None
     if not args.no_fp64:
         ctx64, _ = make_ctx(G, les_cases, shape, h, solid, f, dev, args.precond)
@@ -609,7 +615,8 @@ def run_ours(args):
                        "cells": n, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "flushed (256 MiB write) before every timed step",
                        "inner_rtol": args.inner_rtol, "tma": args.tma, "fused": args.fused,
-                       "rows": args.rows, "chunks": args.chunks, "graph": args.graph},
+                       "rows": args.rows, "chunks": args.chunks, "graph": args.graph,
+                       "pdl": args.pdl, "autotune_us": tune_us},
             "e2e": e2e, "gpu_launches": launches, "wall_s": wall,
             "iters_inner_mean": statistics.mean(rec["iters"]), "outer_mean": statistics.mean(rec["outer"]),
             "rel_residual_max": max(rec["rres"]), "roofline": roof, "clocks": clk}

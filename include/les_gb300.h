@@ -344,10 +344,14 @@ typedef enum les_option {
                              (Chebyshev degree 2..4), 4 (degree 5..7) */
     LES_OPT_CHUNK_A = 4,  /* planes per march chunk of pass A */
     LES_OPT_CHUNK_B = 5,  /* planes per march chunk of pass B */
-    LES_OPT_GRAPH = 6     /* 1 (default): les_step with the mixed-precision fused PCG
+    LES_OPT_GRAPH = 6,    /* 1 (default): les_step with the mixed-precision fused PCG
                              runs as one CUDA graph launch (captured per velocity
                              buffer parity, both solver loops as conditional nodes;
                              not while les_profile records); 0: launch by launch */
+    LES_OPT_PDL = 7       /* 1 (default): the register-column passes are launched as
+                             programmatic dependents of the kernel before them (their
+                             blocks become resident while it drains); 0: plain
+                             stream order */
 } les_option;
 les_status les_set_option(les_ctx* ctx, int option, int value);
 

@@ -112,14 +112,15 @@ __global__ void __launch_bounds__(CT, TJ == 8 ? 4 : 2) k_col_a(Geo g, ColMap m, 
 {
     constexpr int H = TJ + 2;
     __shared__ double sm[32];
+    const int lane = threadIdx.x & 31;
+    const int item = blockIdx.x * CWPB + (threadIdx.x >> 5);
+    const StripPos s = strip_pos<1, TJ>(g, m, item, lane);   // from the arguments only
+    dep_wait();
     if (st->done) return;
     const float beta = FIRST ? 0.f : (float)st->beta;
     const float aprev = FIRST ? 0.f : (float)st->alpha;
-    const int lane = threadIdx.x & 31;
-    const int item = blockIdx.x * CWPB + (threadIdx.x >> 5);
     Acc acc;
     if (item < m.items) {
-        const StripPos s = strip_pos<1, TJ>(g, m, item, lane);
         float p0[H], p1[H], p2[H];   // p at planes P, P-1, P-2
         float vz[H], vp[H], ve[TJ];  // z, p_old, e of the plane being fetched
 #pragma unroll
@@ -196,6 +197,7 @@ __global__ void __launch_bounds__(CT, TJ == 8 ? 4 : 2) k_col_a(Geo g, ColMap m, 
             }
         }
     }
+    dep_signal();
     double v[1] = {acc_value(acc)};
     if (last_block_sum<1>(v, partials, counter, sm)) {
         if (threadIdx.x == 0) {
@@ -244,13 +246,14 @@ __global__ void __launch_bounds__(CT, (TJ == 4 && S <= 3) ? 3 : 2) k_col_b(Geo g
     constexpr int H = TJ + 2 * S;
     constexpr int NL = S > 1 ? S - 1 : 1;   // stored levels z_1 .. z_{S-1}
     __shared__ double sm[64];
-    if (st->done) return;
-    const float alpha = FIRST ? 0.f : (float)st->alpha;
     const int lane = threadIdx.x & 31;
     const int item = blockIdx.x * CWPB + (threadIdx.x >> 5);
+    const StripPos s = strip_pos<S, TJ>(g, m, item, lane);   // from the arguments only
+    dep_wait();
+    if (st->done) return;
+    const float alpha = FIRST ? 0.f : (float)st->alpha;
     Acc arr, arz;
     if (item < m.items) {
-        const StripPos s = strip_pos<S, TJ>(g, m, item, lane);
         float rp[S + 1][H];      // r' at planes I - d
         float zr[NL][3][H];      // z_L at planes I - L - d (L = 1 .. S-1 at [L-1])
         float pcr[NL][2][H];     // pc_L at planes I - L - d
@@ -384,6 +387,7 @@ __global__ void __launch_bounds__(CT, (TJ == 4 && S <= 3) ? 3 : 2) k_col_b(Geo g
                 }
         }
     }
+    dep_signal();
     pass_b_finish<FIRST>(arr, arz, partials, counter, sm, st, outer, total_cap);
 }
 
@@ -504,7 +508,7 @@ static Coef coef_of(const ColPlan& P) { return Coef{P.A.k.c0, P.A.k.x1, P.A.k.y1
 les_status col_pass_a(les_ctx* c, const ColPlan& P, bool first, int pc)
 {
     float *z = c->f[1], *pb[2] = {c->f[2], c->f[3]}, *q = c->f[4], *e = c->f[5];
-    launch_p(c, PROF_IN_SPMV, pick_a(P.ma.tj, first), P.blocks_a, CT, c->g, P.ma, coef_of(P), (const float*)z,
+    launch_pdl(c, PROF_IN_SPMV, pick_a(P.ma.tj, first), P.blocks_a, CT, c->g, P.ma, coef_of(P), (const float*)z,
              (const float*)pb[pc], pb[pc ^ 1], q, e, c->partials, c->counters + 15, P.in, pc ^ 1);
     return check_launch(c, "column pass A");
 }
@@ -513,7 +517,7 @@ les_status col_pass_b(les_ctx* c, const ColPlan& P, bool first, int rin)
 {
     float* r[2] = {c->f[0], c->f[6]};
     float *z = c->f[1], *q = c->f[4];
-    launch_p(c, PROF_IN_CHEB, pick_b(P.S, P.mb.tj, first), P.blocks_b, CT, c->g, P.mb, coef_of(P), P.cf, P.inv_c0,
+    launch_pdl(c, PROF_IN_CHEB, pick_b(P.S, P.mb.tj, first), P.blocks_b, CT, c->g, P.mb, coef_of(P), P.cf, P.inv_c0,
              (const float*)r[rin], r[rin ^ 1], (const float*)q, z, c->partials, c->counters + 14, P.in, P.out, P.cap);
     return check_launch(c, "column pass B");
 }

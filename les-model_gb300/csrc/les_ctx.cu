@@ -346,6 +346,7 @@ les_status les_set_option(les_ctx* c, int option, int value)
     ++c->version;   // captured step graphs depend on every option
     switch (option) {
     case LES_OPT_GRAPH: c->graph_on = value ? 1 : 0; return LES_OK;
+    case LES_OPT_PDL: c->pdl = value ? 1 : 0; return LES_OK;
     case LES_OPT_FUSED: c->fused = value == 2 ? 2 : (value ? 1 : 0); return LES_OK;
     case LES_OPT_TMA: c->opt_tma = value ? 1 : 0; return LES_OK;
     case LES_OPT_ROWS_A: c->tune_tja = value; return LES_OK;

@@ -312,6 +312,7 @@ struct les_ctx {
     // CUDA-graph time steps (les_step.cu): one executable graph per velocity
     // buffer parity, rebuilt when anything baked into it changes
     int graph_on = 1;                     // LES_OPT_GRAPH
+    int pdl = 1;                          // LES_OPT_PDL
     cudaStream_t aux = nullptr;           // capture stream for conditional-loop bodies
     struct les::StepGraph* sg[2] = {};
     int sg_last = 0;                      // slot of the graph launched last
@@ -352,6 +353,34 @@ inline void launch_p(les_ctx* c, int pid, void (*k)(KArgs...), dim3 grid, dim3 b
     ++c->launches;
     if (e1) cudaEventRecord(e1, c->stream);
 }
+
+// Same, as a programmatic dependent launch when c->pdl is set: the kernel may
+// start while the kernel before it in the stream drains, so it must execute
+// dep_wait() before its first access to device memory.
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(les_ctx* c, int pid, void (*k)(KArgs...), dim3 grid, dim3 block, Args... args)
+{
+    cudaEvent_t e1 = nullptr;
+    if (c->prof_on) prof_begin(c, pid, &e1);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.stream = c->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = c->pdl ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...);
+    ++c->launches;
+    if (e1) cudaEventRecord(e1, c->stream);
+}
+
+// Waits until the grids this one depends on have completed and their writes
+// are visible (returns at once for a kernel launched in plain stream order).
+__device__ __forceinline__ void dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// Lets the dependent grid launch once every block has signalled or exited.
+__device__ __forceinline__ void dep_signal() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 }  // namespace les
 

@@ -103,12 +103,13 @@ def test_small_config_steps_match_oracle(oracle_lib):
         assert same(c.download_mask(), solid)
 
 
-def _mixed_run(shape, solid, f, lmax, steps, graph, fused=1, dt_fixed=0.0):
+def _mixed_run(shape, solid, f, lmax, steps, graph, fused=1, dt_fixed=0.0, pdl=1):
     h = 1.0 / 32
     m = G.Mesh(*shape, h, h, h)
     with G.Context(m) as c:
         c.set_option(G.OPT_GRAPH, graph)
         c.set_option(G.OPT_FUSED, fused)
+        c.set_option(G.OPT_PDL, pdl)
         c.upload_mask(np.zeros(m.n, np.uint8))
         c.build_stencil()
         c.upload_fields(f)
@@ -147,4 +148,25 @@ def test_graph_step_matches_launch_by_launch(shape, fused, dt_fixed):
     s1, f1 = _mixed_run(shape, solid, f, lmax, 5, 1, fused, dt_fixed)
     assert s0 == s1, (s0, s1)
     for k in ("u", "v", "w", "p", "nu_t", "u_new", "p_rhs"):
+        assert same(f0[k], f1[k]), k
+
+
+@pytest.mark.parametrize("graph", [0, 1], ids=["launches", "graph"])
+def test_dependent_launch_changes_nothing(graph):
+    """The column passes as programmatic dependent launches (each waits for
+    the grid before it ahead of its first memory access) give bit-identical
+    steps to plain stream order, launch by launch and inside the step graph."""
+    shape = (48, 40, 36)
+    n = int(np.prod(shape))
+    solid = les_cases.box_mask(shape, (12, 16, 12, 18, 10, 16))
+    f = les_cases.init_fields(shape, 0.01, 77)
+    h = 1.0 / 32
+    with G.Context(G.Mesh(*shape, h, h, h)) as c:
+        c.upload_mask(np.zeros(n, np.uint8))
+        c.build_stencil()
+        lmax = c.lambda_max(20)
+    s0, f0 = _mixed_run(shape, solid, f, lmax, 4, graph, pdl=0)
+    s1, f1 = _mixed_run(shape, solid, f, lmax, 4, graph, pdl=1)
+    assert s0 == s1, (s0, s1)
+    for k in ("u", "v", "w", "p", "nu_t"):
         assert same(f0[k], f1[k]), k
