@@ -73,6 +73,7 @@ def parse():
     ap.add_argument("--chunks", default="0,0", help="planes per march chunk of the column passes A,B (0 = auto)")
     ap.add_argument("--graph", type=int, default=1, help="replay each time step as one CUDA graph (LES_OPT_GRAPH)")
     ap.add_argument("--pdl", type=int, default=1, help="column passes as programmatic dependent launches (LES_OPT_PDL)")
+    ap.add_argument("--phys32", type=int, default=1, help="mixed path: nu_t and momentum in FP32 (LES_OPT_PHYS32)")
     ap.add_argument("--prof-steps", type=int, default=2, help="extra steps timed per kernel for the roofline")
     return ap.parse_args()
 
@@ -488,6 +489,7 @@ def run_ours(args):
     ctx.set_option(G.OPT_TMA, args.tma)
     ctx.set_option(G.OPT_GRAPH, args.graph)
     ctx.set_option(G.OPT_PDL, args.pdl)
+    ctx.set_option(G.OPT_PHYS32, args.phys32)
     ra, rb = (int(x) for x in args.rows.split(","))
     ca, cb = (int(x) for x in args.chunks.split(","))
     for opt, v in ((G.OPT_ROWS_A, ra), (G.OPT_ROWS_B, rb), (G.OPT_CHUNK_A, ca), (G.OPT_CHUNK_B, cb)):
@@ -616,7 +618,7 @@ def run_ours(args):
                        "l2": "flushed (256 MiB write) before every timed step",
                        "inner_rtol": args.inner_rtol, "tma": args.tma, "fused": args.fused,
                        "rows": args.rows, "chunks": args.chunks, "graph": args.graph,
-                       "pdl": args.pdl, "autotune_us": tune_us},
+                       "pdl": args.pdl, "phys32": args.phys32, "autotune_us": tune_us},
             "e2e": e2e, "gpu_launches": launches, "wall_s": wall,
             "iters_inner_mean": statistics.mean(rec["iters"]), "outer_mean": statistics.mean(rec["outer"]),
             "rel_residual_max": max(rec["rres"]), "roofline": roof, "clocks": clk}

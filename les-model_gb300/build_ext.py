@@ -23,6 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = {
     "les_ctx.cu": ["-fmad=false"],
     "les_physics.cu": ["-fmad=false"],
+    "les_physics32.cu": [],
     "les_pressure.cu": ["-fmad=false"],
     "les_wavefront.cu": ["-fmad=false"],
     "les_mixed.cu": [],

@@ -544,11 +544,15 @@ __global__ void k_tl_objective(Geo g, int i0, int i1, int j0, int j1, int k0, in
         if (threadIdx.x == 0 && threadIdx.y == 0) acc[0] += scale * e[0];
 }
 
-// one forward step with the checks the gradient relies on
+// one forward step with the checks the gradient relies on; the physics is
+// the FP64 one that the adjoint and tangent kernels differentiate
 les_status fwd_step(les_ctx* c, const les_step_params* prm)
 {
     les_step_stats s{};
+    const int phys32 = c->phys32;
+    c->phys32 = 0;
     les_status st = les_step(c, prm, &s);
+    c->phys32 = phys32;
     if (st) return st;
     if (s.status != LES_OK) return fail(c, (les_status)s.status, "adjoint: a forward pressure solve did not converge");
     return LES_OK;

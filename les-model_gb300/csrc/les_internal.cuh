@@ -313,6 +313,7 @@ struct les_ctx {
     // buffer parity, rebuilt when anything baked into it changes
     int graph_on = 1;                     // LES_OPT_GRAPH
     int pdl = 1;                          // LES_OPT_PDL
+    int phys32 = 1;                       // LES_OPT_PHYS32
     cudaStream_t aux = nullptr;           // capture stream for conditional-loop bodies
     struct les::StepGraph* sg[2] = {};
     int sg_last = 0;                      // slot of the graph launched last

@@ -15,6 +15,8 @@ namespace les {
 les_status velocity_bcs_dev(les_ctx* c);
 les_status sgs_nut_dev(les_ctx* c, double cs, int want_tau);
 les_status momentum_dev(les_ctx* c, double dt, double nu, const double* dtp);
+les_status sgs_nut32_dev(les_ctx* c, double cs);
+les_status momentum32_dev(les_ctx* c, double dt, double nu, const double* dtp);
 les_status correct_dev(les_ctx* c, double dt, double rho, const double* dtp);
 les_status adaptive_dt_dev(les_ctx* c, double nu, double cfl_conv, double cfl_visc, double dt_max);
 les_status div_b_dev(les_ctx* c, double dt, double rho, double rel_tol, const double* dtp);
@@ -36,6 +38,7 @@ struct StepGraph {
     les_step_params prm{};
     double* slots[LES_NSLOTS] = {};
     double* tau = nullptr;
+    int phys32 = 0;
     unsigned long long version = 0;
     cudaGraphExec_t exec = nullptr;
     unsigned long long captured = 0;   // kernel nodes outside and inside one pass of each loop
@@ -52,6 +55,24 @@ bool graph_eligible(const les_ctx* c, const les_step_params* prm)
 {
     return !c->prof_on && prm->solver == LES_SOLVER_PCG && prm->pcg.precision == LES_MIXED &&
            c->stencil_mode == 1 && c->fused && fused_supported(&prm->pcg) && prm->pcg.max_iter > 0;
+}
+
+// FP32 physics (les_physics32.cu) for a step of the mixed-precision solve
+bool phys32_on(const les_ctx* c, const les_step_params* prm)
+{
+    return c->phys32 && prm->solver == LES_SOLVER_PCG && prm->pcg.precision == LES_MIXED && !prm->want_tau;
+}
+
+// nu_t (with its boundary values) and the momentum update of one step
+les_status physics_dev(les_ctx* c, const les_step_params* prm, double dt, const double* dtp)
+{
+    les_status st;
+    if (phys32_on(c, prm)) {
+        if ((st = sgs_nut32_dev(c, prm->cs))) return st;
+        return momentum32_dev(c, dt, prm->nu, dtp);
+    }
+    if ((st = sgs_nut_dev(c, prm->cs, prm->want_tau))) return st;
+    return momentum_dev(c, dt, prm->nu, dtp);
 }
 
 void swap_velocity(les_ctx* c)
@@ -87,7 +108,7 @@ unsigned long long graph_step_stats(les_ctx* c, const les_step_params* prm, unsi
 
 static bool graph_matches(const les_ctx* c, const StepGraph* s, const les_step_params* prm)
 {
-    return s && s->exec && s->version == c->version && s->tau == c->tau &&
+    return s && s->exec && s->version == c->version && s->tau == c->tau && s->phys32 == c->phys32 &&
            std::memcmp(&s->prm, prm, sizeof *prm) == 0 && std::memcmp(s->slots, c->slot, sizeof s->slots) == 0;
 }
 
@@ -102,8 +123,7 @@ les_status les::emit_step(les_ctx* c, const les_step_params* prm)
         dtp = &c->state[0].scal[0];   // nothing else in the step writes it
         dt = 1.0;                     // unused: the kernels read *dtp
     }
-    if ((st = sgs_nut_dev(c, prm->cs, prm->want_tau))) return st;
-    if ((st = momentum_dev(c, dt, prm->nu, dtp))) return st;
+    if ((st = physics_dev(c, prm, dt, dtp))) return st;
     if ((st = velocity_bcs_dev(c))) return st;
     if ((st = div_b_dev(c, dt, prm->rho, prm->rel_tol, dtp))) return st;
     if ((st = capture_mixed_fused(c, &prm->pcg, view32_of(c), prm->rel_tol > 0 ? 1 : 0))) return st;
@@ -122,7 +142,8 @@ static les_status step_graph(les_ctx* c, const les_step_params* prm, les_step_st
         // capture into an empty or stale slot, else replace the graph not used last
         int k = -1;
         for (int q = 0; q < 2 && k < 0; ++q)
-            if (!c->sg[q] || c->sg[q]->version != c->version || std::memcmp(&c->sg[q]->prm, prm, sizeof *prm) != 0)
+            if (!c->sg[q] || c->sg[q]->version != c->version || c->sg[q]->phys32 != c->phys32 ||
+                std::memcmp(&c->sg[q]->prm, prm, sizeof *prm) != 0)
                 k = q;
         if (k < 0) k = c->sg_last ^ 1;
         step_graph_free(c->sg[k]);
@@ -130,6 +151,7 @@ static les_status step_graph(les_ctx* c, const les_step_params* prm, les_step_st
         g->prm = *prm;
         std::memcpy(g->slots, c->slot, sizeof g->slots);
         g->version = c->version;
+        g->phys32 = c->phys32;
         double* before[LES_NSLOTS];
         std::memcpy(before, c->slot, sizeof before);
         const unsigned long long l0 = c->launches;
@@ -182,8 +204,7 @@ extern "C" les_status les_step(les_ctx* c, const les_step_params* prm, les_step_
         if (st) return st;
         dt = c->h_state[0].scal[0];
     }
-    if ((st = sgs_nut_dev(c, prm->cs, prm->want_tau))) return st;
-    if ((st = momentum_dev(c, dt, prm->nu, nullptr))) return st;
+    if ((st = physics_dev(c, prm, dt, nullptr))) return st;
     if ((st = velocity_bcs_dev(c))) return st;
     les_status solve = LES_OK;
     les_step_stats s{};

@@ -170,3 +170,44 @@ def test_dependent_launch_changes_nothing(graph):
     assert s0 == s1, (s0, s1)
     for k in ("u", "v", "w", "p", "nu_t"):
         assert same(f0[k], f1[k]), k
+
+
+def test_fp32_physics_step_close_to_fp64_physics():
+    """nu_t and the momentum update in FP32 (LES_OPT_PHYS32, the mixed path's
+    default) against the reference-order FP64 kernels, both with the mixed
+    pressure solve: same solver work, and velocity, pressure and nu_t within
+    the FP32 rounding of the tendencies (the velocity update itself is FP64)."""
+    shape = (64, 32, 32)
+    n = int(np.prod(shape))
+    solid = les_cases.box_mask(shape, (16, 24, 12, 20, 12, 20))
+    f = les_cases.init_fields(shape, 0.01, 1234)
+    h = 1.0 / 32
+    with G.Context(G.Mesh(*shape, h, h, h)) as c:
+        c.upload_mask(np.zeros(n, np.uint8))
+        c.build_stencil()
+        lmax = c.lambda_max(20)
+    res = {}
+    for p32 in (0, 1):
+        m = G.Mesh(*shape, h, h, h)
+        with G.Context(m) as c:
+            c.set_option(G.OPT_PHYS32, p32)
+            c.upload_mask(np.zeros(n, np.uint8))
+            c.build_stencil()
+            c.upload_fields(f)
+            c.upload_mask(solid)
+            c.velocity_bcs()
+            prm = G.step_params(nu=les_cases.NU, rho=les_cases.RHO, cs=les_cases.CS, cfl_conv=les_cases.CFL_CONV,
+                                solver=G.SOLVER_PCG, rel_tol=1e-8,
+                                pcg=G.pcg_opts(precond=G.PC_CHEBYSHEV, max_iter=5000, lambda_min=3 * np.pi ** 2,
+                                               lambda_max=lmax, degree=4, precision=G.MIXED, inner_rtol=1e-4))
+            stats = [c.step(prm) for _ in range(6)]
+            res[p32] = (stats, c.download_fields(("u", "v", "w", "p", "nu_t")))
+    (s0, f0), (s1, f1) = res[0], res[1]
+    for a, b in zip(s0, s1):
+        assert a.status == G.OK and b.status == G.OK
+        assert abs(a.iters - b.iters) <= 2, (a.iters, b.iters)
+        assert abs(a.dt - b.dt) <= 1e-6 * a.dt
+    for k, bar in (("u", 1e-7), ("v", 1e-7), ("w", 1e-7), ("p", 1e-6), ("nu_t", 1e-4)):
+        scale = max(np.max(np.abs(f0[k])), 1e-300)
+        err = np.max(np.abs(f1[k] - f0[k])) / scale
+        assert err < bar, (k, err)
