@@ -16,12 +16,13 @@
 // system has no null space (the outlet rows are Dirichlet), so there is no
 // mean-pressure removal step.
 //
-// FP32 kernels here may contract a*b+c into FMA (this file is compiled
-// without -fmad=false); the FP64 residual kernel keeps the reference's
-// rounding by using explicit __dmul_rn/__dadd_rn.
+// Kernels here may contract a*b+c into FMA (this file is compiled without
+// -fmad=false): the FP64 defect is a sum of fused multiply-adds, at least as
+// accurate as the reference's separately rounded products.
 #include <cmath>
 #include <utility>
 
+#include "les_bits.cuh"
 #include "les_internal.cuh"
 #include "les_mixed.cuh"
 
@@ -43,18 +44,28 @@ __device__ __forceinline__ bool cell_coords(const Geo& g, int& i, int& j, int& k
 }
 
 
+// (A x)_id in FP64 fused multiply-adds (GB300 runs about 2 FP64 instructions
+// per SM and clock, so the defect is bound by their count)
 __device__ __forceinline__ double row64(const StencilView& A, const double* __restrict__ x, const Geo& g,
                                         int i, int j, int k, int id)
 {
     Coef7 a = A.at(id);
-    double val = __dmul_rn(a.c, x[id]);
-    if (i > 0) val = __dadd_rn(val, __dmul_rn(a.w, x[id - g.si]));
-    if (i < g.nx - 1) val = __dadd_rn(val, __dmul_rn(a.e, x[id + g.si]));
-    if (j > 0) val = __dadd_rn(val, __dmul_rn(a.s, x[id - g.sj]));
-    if (j < g.ny - 1) val = __dadd_rn(val, __dmul_rn(a.n, x[id + g.sj]));
-    if (k > 0) val = __dadd_rn(val, __dmul_rn(a.b, x[id - 1]));
-    if (k < g.nz - 1) val = __dadd_rn(val, __dmul_rn(a.t, x[id + 1]));
+    double val = a.c * x[id];
+    if (i > 0) val = fma(a.w, x[id - g.si], val);
+    if (i < g.nx - 1) val = fma(a.e, x[id + g.si], val);
+    if (j > 0) val = fma(a.s, x[id - g.sj], val);
+    if (j < g.ny - 1) val = fma(a.n, x[id + g.sj], val);
+    if (k > 0) val = fma(a.b, x[id - 1], val);
+    if (k < g.nz - 1) val = fma(a.t, x[id + 1], val);
     return val;
+}
+
+constexpr int RES_PLANES = 4;   // planes per thread of the defect kernel
+
+inline dim3 resid_grid(const Geo& g)
+{
+    const dim3 c = cell_grid(g);
+    return dim3(c.x, c.y, (g.nx + RES_PLANES - 1) / RES_PLANES);
 }
 
 // Outer residual: r = b - A x in FP64, its FP32 copy for the inner solve, and
@@ -66,11 +77,14 @@ __global__ void k_outer_resid(Geo g, StencilView A, const double* __restrict__ x
     __shared__ double sm[32];
     int i, j, k;
     double rr[1] = {0.0};
-    if (cell_coords(g, i, j, k)) {
-        const int id = i * g.si + j * g.sj + k;
-        double r = __dadd_rn(b[id], -row64(A, x, g, i, j, k, id));
-        r32[id] = (float)r;
-        rr[0] = __dmul_rn(r, r);
+    if (cell_coords(g, i, j, k)) {   // blockIdx.z: a group of RES_PLANES planes
+        const int i0 = i * RES_PLANES, i1 = min(g.nx, i0 + RES_PLANES);
+        for (i = i0; i < i1; ++i) {
+            const int id = i * g.si + j * g.sj + k;
+            const double r = b[id] - row64(A, x, g, i, j, k, id);
+            r32[id] = d2f_bits(r);
+            rr[0] = fma(r, r, rr[0]);
+        }
     }
     if (last_block_sum<1>(rr, partials, counter, sm)) {
         if (threadIdx.x == 0 && threadIdx.y == 0) {
@@ -396,7 +410,7 @@ les_status pcg_mixed_impl(les_ctx* c, const les_pcg_opts* o, les_pcg_result* res
     const int max_outer = o->max_outer > 0 ? o->max_outer : 50;
 
     launch(c, k_set_outer, 1, 1, out, o->tol, keep_tol);
-    launch_p(c, PROF_OUTER, k_outer_resid, gr, bl, g, A, x, b, r, c->partials, c->counters + 8, out, 0);
+    launch_p(c, PROF_OUTER, k_outer_resid, resid_grid(g), bl, g, A, x, b, r, c->partials, c->counters + 8, out, 0);
     st = check_launch(c, "outer residual");
     if (st) return st;
     st = read_state(c);
@@ -455,7 +469,7 @@ les_status pcg_mixed_impl(les_ctx* c, const les_pcg_opts* o, les_pcg_result* res
             launch(c, k_x_add, gr, bl, g, x, e);
         }
         ++outer;
-        launch_p(c, PROF_OUTER, k_outer_resid, gr, bl, g, A, x, b, r, c->partials, c->counters + 8, out, outer);
+        launch_p(c, PROF_OUTER, k_outer_resid, resid_grid(g), bl, g, A, x, b, r, c->partials, c->counters + 8, out, outer);
         st = check_launch(c, "outer correction");
         if (st) return st;
         st = read_state(c);
@@ -480,7 +494,7 @@ les_status emit_outer_start(les_ctx* c, const les_pcg_opts* o, int keep_tol)
 {
     const Geo& g = c->g;
     launch(c, k_set_outer, 1, 1, c->state, o->tol, keep_tol);
-    launch_p(c, PROF_OUTER, k_outer_resid, cell_grid(g), cell_block(), g, stencil_view(c), (const double*)c->slot[LES_P],
+    launch_p(c, PROF_OUTER, k_outer_resid, resid_grid(g), cell_block(), g, stencil_view(c), (const double*)c->slot[LES_P],
              (const double*)c->slot[LES_B], c->f[0], c->partials, c->counters + 8, c->state, 0);
     return check_launch(c, "outer start");
 }
@@ -500,7 +514,7 @@ les_status emit_outer_update(les_ctx* c, bool deferred)
     } else {
         launch(c, k_x_add, cell_grid(g), cell_block(), g, c->slot[LES_P], (const float*)c->f[5]);
     }
-    launch_p(c, PROF_OUTER, k_outer_resid, cell_grid(g), cell_block(), g, stencil_view(c), (const double*)c->slot[LES_P],
+    launch_p(c, PROF_OUTER, k_outer_resid, resid_grid(g), cell_block(), g, stencil_view(c), (const double*)c->slot[LES_P],
              (const double*)c->slot[LES_B], c->f[0], c->partials, c->counters + 8, c->state, -1);
     return check_launch(c, "outer update");
 }

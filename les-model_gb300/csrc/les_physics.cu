@@ -215,6 +215,27 @@ __global__ void k_correct(Geo g, StepConst s, double dt_over_rho, const double* 
     w[id] -= dt_over_rho * ((p[id + 1] - p[id - 1]) * s.inv_2dz);
 }
 
+// Running maximum of non-negative doubles as unsigned integers: for such
+// values the order of the bit patterns is the order of the numbers, and the
+// integer pipe is far faster than GB300's FP64 one.  What the reference's
+// `(m < x) ? x : m` never selects from a start of 0 -- NaN and negative
+// values -- maps to 0 (+0.0).
+__device__ __forceinline__ unsigned long long max_key(double x)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    return b > 0x7ff0000000000000ull ? 0ull : b;   // sign bit set or NaN
+}
+
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long t = __shfl_down_sync(0xffffffffu, v, o);
+        v = t > v ? t : v;
+    }
+    return v;
+}
+
 // compute_adaptive_dt, src/main.cpp:208-250: max |u|^2 and max nu_t over
 // all cells (max is exact, so the reduction order does not matter), then the
 // final formula in the last block.
@@ -223,49 +244,49 @@ __global__ void k_dt(Geo g, const double* __restrict__ u, const double* __restri
                      double* partials, unsigned* counter, SolverState* st, double nu,
                      double cfl_conv, double cfl_visc, double dt_max, double min_dx)
 {
-    __shared__ double sm[2][32];
+    __shared__ unsigned long long sm[2][32];
     __shared__ int am_last;
     int i, j, k;
-    double m2 = 0.0, mt = 0.0;
+    unsigned long long m2 = 0ull, mt = 0ull;
     if (cell_coords(g, i, j, k)) {
         int id = i * g.si + j * g.sj + k;
         double mag = u[id] * u[id] + v[id] * v[id] + w[id] * w[id];
-        m2 = (m2 < mag) ? mag : m2;
-        mt = (mt < nu_t[id]) ? nu_t[id] : mt;
+        m2 = max_key(mag);
+        mt = max_key(nu_t[id]);
     }
     const int tid = threadIdx.x + blockDim.x * threadIdx.y, lane = tid & 31, warp = tid >> 5;
-    m2 = warp_max(m2);
-    mt = warp_max(mt);
+    m2 = warp_max_u64(m2);
+    mt = warp_max_u64(mt);
     if (lane == 0) { sm[0][warp] = m2; sm[1][warp] = mt; }
     __syncthreads();
     const int nw = (blockDim.x * blockDim.y) >> 5, nb = block_count(), bid = block_linear_id();
+    unsigned long long* pk = reinterpret_cast<unsigned long long*>(partials);
     if (tid == 0) {
-        double a = 0.0, b = 0.0;
-        for (int q = 0; q < nw; ++q) { a = fmax(a, sm[0][q]); b = fmax(b, sm[1][q]); }
-        partials[bid] = a;
-        partials[nb + bid] = b;
+        unsigned long long a = 0ull, b = 0ull;
+        for (int q = 0; q < nw; ++q) { a = sm[0][q] > a ? sm[0][q] : a; b = sm[1][q] > b ? sm[1][q] : b; }
+        pk[bid] = a;
+        pk[nb + bid] = b;
         __threadfence();
         am_last = atomicAdd(counter, 1u) == (unsigned)nb - 1u;
     }
     __syncthreads();
     if (!am_last) return;
     __threadfence();
-    double a = 0.0, b = 0.0;
+    unsigned long long a = 0ull, b = 0ull;
     for (int q = tid; q < nb; q += blockDim.x * blockDim.y) {
-        a = fmax(a, __ldcg(partials + q));
-        b = fmax(b, __ldcg(partials + nb + q));
+        const unsigned long long pa = __ldcg(pk + q), pb = __ldcg(pk + nb + q);
+        a = pa > a ? pa : a;
+        b = pb > b ? pb : b;
     }
-    a = warp_max(a);
-    b = warp_max(b);
+    a = warp_max_u64(a);
+    b = warp_max_u64(b);
     __syncthreads();
     if (lane == 0) { sm[0][warp] = a; sm[1][warp] = b; }
     __syncthreads();
     if (tid == 0) {
-        double u_max_sq = 0.0, nu_t_max = 0.0;
-        for (int q = 0; q < nw; ++q) {
-            u_max_sq = (u_max_sq < sm[0][q]) ? sm[0][q] : u_max_sq;
-            nu_t_max = (nu_t_max < sm[1][q]) ? sm[1][q] : nu_t_max;
-        }
+        unsigned long long ka = 0ull, kb = 0ull;
+        for (int q = 0; q < nw; ++q) { ka = sm[0][q] > ka ? sm[0][q] : ka; kb = sm[1][q] > kb ? sm[1][q] : kb; }
+        const double u_max_sq = __longlong_as_double((long long)ka), nu_t_max = __longlong_as_double((long long)kb);
         double u_max = sqrt(u_max_sq);
         double dt_conv = 1.7976931348623157e308;
         if (u_max > 1e-12) dt_conv = cfl_conv * min_dx / u_max;
