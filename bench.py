@@ -72,7 +72,9 @@ def parse():
     ap.add_argument("--rows", default="0,0", help="rows per strip of the column passes A,B (0 = built-in)")
     ap.add_argument("--chunks", default="0,0", help="planes per march chunk of the column passes A,B (0 = auto)")
     ap.add_argument("--graph", type=int, default=1, help="replay each time step as one CUDA graph (LES_OPT_GRAPH)")
-    ap.add_argument("--pdl", type=int, default=1, help="column passes as programmatic dependent launches (LES_OPT_PDL)")
+    ap.add_argument("--pdl", type=int, default=None,
+                    help="column passes as programmatic dependent launches (LES_OPT_PDL; default: the library's, "
+                         "on for a single case, off for ensemble cases)")
     ap.add_argument("--phys32", type=int, default=1, help="mixed path: nu_t and momentum in FP32 (LES_OPT_PHYS32)")
     ap.add_argument("--prof-steps", type=int, default=2, help="extra steps timed per kernel for the roofline")
     return ap.parse_args()
@@ -311,6 +313,9 @@ def run_batch(args):
     for c, s in zip(ens.cases, specs):
         shape = s["shape"]
         n = int(np.prod(shape))
+        if args.pdl is not None:
+            c.set_option(G.OPT_PDL, args.pdl)
+        c.set_option(G.OPT_PHYS32, args.phys32)
         c.upload_mask(np.zeros(n, np.uint8))
         c.build_stencil()
         lmax = c.lambda_max(20)
@@ -367,6 +372,7 @@ def run_batch(args):
                        "parallelism": "cases sharded over %d ranks, no exchange" % world if world > 1 else "single",
                        "timing": "host wall clock around each step's launch + stats sync, max over ranks",
                        "l2": "inputs (~%.1f GB) larger than L2" % (cells * 120 / 1e9),
+                       "pdl": 0 if args.pdl is None else args.pdl, "phys32": args.phys32,
                        "autotune_us_per_iteration": tune_us, "autotune_s": tune_s,
                        "first_steps_with_capture_s": warm_s},
             "gpu_launches": launches, "iters_inner_mean": statistics.mean(iters), "rel_residual_max": worst,
@@ -488,7 +494,7 @@ def run_ours(args):
     ctx.set_option(G.OPT_FUSED, args.fused)
     ctx.set_option(G.OPT_TMA, args.tma)
     ctx.set_option(G.OPT_GRAPH, args.graph)
-    ctx.set_option(G.OPT_PDL, args.pdl)
+    ctx.set_option(G.OPT_PDL, 1 if args.pdl is None else args.pdl)
     ctx.set_option(G.OPT_PHYS32, args.phys32)
     ra, rb = (int(x) for x in args.rows.split(","))
     ca, cb = (int(x) for x in args.chunks.split(","))
@@ -618,7 +624,8 @@ def run_ours(args):
                        "l2": "flushed (256 MiB write) before every timed step",
                        "inner_rtol": args.inner_rtol, "tma": args.tma, "fused": args.fused,
                        "rows": args.rows, "chunks": args.chunks, "graph": args.graph,
-                       "pdl": args.pdl, "phys32": args.phys32, "autotune_us": tune_us},
+                       "pdl": 1 if args.pdl is None else args.pdl, "phys32": args.phys32,
+                       "autotune_us": tune_us},
             "e2e": e2e, "gpu_launches": launches, "wall_s": wall,
             "iters_inner_mean": statistics.mean(rec["iters"]), "outer_mean": statistics.mean(rec["outer"]),
             "rel_residual_max": max(rec["rres"]), "roofline": roof, "clocks": clk}

@@ -348,10 +348,10 @@ typedef enum les_option {
                              runs as one CUDA graph launch (captured per velocity
                              buffer parity, both solver loops as conditional nodes;
                              not while les_profile records); 0: launch by launch */
-    LES_OPT_PDL = 7,      /* 1 (default): the register-column passes are launched as
-                             programmatic dependents of the kernel before them (their
-                             blocks become resident while it drains); 0: plain
-                             stream order */
+    LES_OPT_PDL = 7,      /* 1 (default; 0 for ensemble cases): the register-column
+                             passes are launched as programmatic dependents of the
+                             kernel before them (their blocks become resident while it
+                             drains); 0: plain stream order */
     LES_OPT_PHYS32 = 8    /* 1 (default): a les_step whose pressure solve is the
                              mixed-precision PCG computes nu_t and the momentum update
                              in FP32 (FP64 fields, FP64 velocity update; not with
