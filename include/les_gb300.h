@@ -134,6 +134,12 @@ uint8_t* les_mask_ptr(les_ctx* ctx);
 /* ---- host <-> device (the shim's Field sync points) --------------------- */
 les_status les_upload(les_ctx* ctx, int slot, const double* host);
 les_status les_download(les_ctx* ctx, int slot, double* host);
+/* Several slots in one call: one asynchronous copy per slot on the
+ * context's stream, one synchronisation at the end (the host buffers are
+ * free again when the call returns).  Pinned host buffers let the copies run
+ * at the link's bandwidth. */
+les_status les_upload_many(les_ctx* ctx, int count, const int* slots, const double* const* hosts);
+les_status les_download_many(les_ctx* ctx, int count, const int* slots, double* const* hosts);
 /* is_solid (src/field.h:22) as one byte per cell, 0 or 1. */
 les_status les_upload_mask(les_ctx* ctx, const uint8_t* solid);
 les_status les_download_mask(les_ctx* ctx, uint8_t* solid);

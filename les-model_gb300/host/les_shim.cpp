@@ -14,12 +14,14 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <initializer_list>
 #include <map>
 #include <memory>
 #include <mutex>
 #include <stdexcept>
 #include <string>
 #include <tuple>
+#include <utility>
 #include <vector>
 
 #include "les_gb300.h"
@@ -101,6 +103,23 @@ Dev& dev_for_n(size_t n)
 void up(Dev& d, int slot, const std::vector<double>& v) { check(d.c, les_upload(d.c, slot, v.data()), "upload"); }
 void down(Dev& d, int slot, std::vector<double>& v) { check(d.c, les_download(d.c, slot, v.data()), "download"); }
 
+// several fields in one call (one synchronisation)
+void ups(Dev& d, std::initializer_list<std::pair<int, const std::vector<double>*>> fs)
+{
+    std::vector<int> sl;
+    std::vector<const double*> p;
+    for (auto& f : fs) { sl.push_back(f.first); p.push_back(f.second->data()); }
+    check(d.c, les_upload_many(d.c, (int)sl.size(), sl.data(), p.data()), "upload");
+}
+
+void downs(Dev& d, std::initializer_list<std::pair<int, std::vector<double>*>> fs)
+{
+    std::vector<int> sl;
+    std::vector<double*> p;
+    for (auto& f : fs) { sl.push_back(f.first); p.push_back(f.second->data()); }
+    check(d.c, les_download_many(d.c, (int)sl.size(), sl.data(), p.data()), "download");
+}
+
 void up_mask(Dev& d, const Field& f)
 {
     std::vector<uint8_t> m(f.is_solid.size());
@@ -150,7 +169,7 @@ double compute_adaptive_dt(const Field& f, const Mesh& m, double nu)
 {
     std::lock_guard<std::mutex> lk(g_mu);
     Dev& d = dev_for(m);
-    up(d, LES_U, f.u); up(d, LES_V, f.v); up(d, LES_W, f.w); up(d, LES_NU_T, f.nu_t);
+    ups(d, {{LES_U, &f.u}, {LES_V, &f.v}, {LES_W, &f.w}, {LES_NU_T, &f.nu_t}});
     double dt = 0;
     check(d.c, les_adaptive_dt(d.c, nu, 0.4, 0.2, 1e-4, &dt), "les_adaptive_dt");   // src/main.cpp:210-212
     return dt;
@@ -160,7 +179,7 @@ void compute_sgs_stress(Field& f, Stress& sgs, const Mesh& m)
 {
     std::lock_guard<std::mutex> lk(g_mu);
     Dev& d = dev_for(m);
-    up(d, LES_U, f.u); up(d, LES_V, f.v); up(d, LES_W, f.w); up(d, LES_NU_T, f.nu_t);
+    ups(d, {{LES_U, &f.u}, {LES_V, &f.v}, {LES_W, &f.w}, {LES_NU_T, &f.nu_t}});
     check(d.c, les_sgs(d.c, 0.18, 1), "les_sgs");   // Cs of src/main.cpp:425
     down(d, LES_NU_T, f.nu_t);
     const size_t n = f.u.size();
@@ -184,31 +203,30 @@ void solve_momentum(Field& f, const Mesh& m, double dt, double nu)
 {
     std::lock_guard<std::mutex> lk(g_mu);
     Dev& d = dev_for(m);
-    up(d, LES_U, f.u); up(d, LES_V, f.v); up(d, LES_W, f.w);
-    up(d, LES_U_NEW, f.u_new); up(d, LES_V_NEW, f.v_new); up(d, LES_W_NEW, f.w_new);
-    up(d, LES_NU_T, f.nu_t);
+    ups(d, {{LES_U, &f.u}, {LES_V, &f.v}, {LES_W, &f.w}, {LES_U_NEW, &f.u_new}, {LES_V_NEW, &f.v_new},
+            {LES_W_NEW, &f.w_new}, {LES_NU_T, &f.nu_t}});
     check(d.c, les_momentum(d.c, dt, nu), "les_momentum");   // includes the swap of :656-658
-    down(d, LES_U, f.u); down(d, LES_V, f.v); down(d, LES_W, f.w);
-    down(d, LES_U_NEW, f.u_new); down(d, LES_V_NEW, f.v_new); down(d, LES_W_NEW, f.w_new);
+    downs(d, {{LES_U, &f.u}, {LES_V, &f.v}, {LES_W, &f.w}, {LES_U_NEW, &f.u_new}, {LES_V_NEW, &f.v_new},
+              {LES_W_NEW, &f.w_new}});
 }
 
 void apply_velocity_BCs(Field& f, const Mesh& m)
 {
     std::lock_guard<std::mutex> lk(g_mu);
     Dev& d = dev_for(m);
-    up(d, LES_U, f.u); up(d, LES_V, f.v); up(d, LES_W, f.w);
+    ups(d, {{LES_U, &f.u}, {LES_V, &f.v}, {LES_W, &f.w}});
     up_mask(d, f);
     check(d.c, les_velocity_bcs(d.c), "les_velocity_bcs");
-    down(d, LES_U, f.u); down(d, LES_V, f.v); down(d, LES_W, f.w);
+    downs(d, {{LES_U, &f.u}, {LES_V, &f.v}, {LES_W, &f.w}});
 }
 
 void correct_velocity(Field& f, const Mesh& m, double dt, double rho)
 {
     std::lock_guard<std::mutex> lk(g_mu);
     Dev& d = dev_for(m);
-    up(d, LES_U, f.u); up(d, LES_V, f.v); up(d, LES_W, f.w); up(d, LES_P, f.p);
+    ups(d, {{LES_U, &f.u}, {LES_V, &f.v}, {LES_W, &f.w}, {LES_P, &f.p}});
     check(d.c, les_correct_velocity(d.c, dt, rho), "les_correct_velocity");
-    down(d, LES_U, f.u); down(d, LES_V, f.v); down(d, LES_W, f.w);
+    downs(d, {{LES_U, &f.u}, {LES_V, &f.v}, {LES_W, &f.w}});
 }
 
 // ---- pressure, src/pressure.cpp ------------------------------------------
@@ -227,7 +245,7 @@ void solve_pressure_jacobi(Field& f, const Mesh& m, double dt, double rho)
 {
     std::lock_guard<std::mutex> lk(g_mu);
     Dev& d = dev_for(m);
-    up(d, LES_U, f.u); up(d, LES_V, f.v); up(d, LES_W, f.w); up(d, LES_P, f.p);
+    ups(d, {{LES_U, &f.u}, {LES_V, &f.v}, {LES_W, &f.w}, {LES_P, &f.p}});
     up_mask(d, f);
     int sweeps = 0;
     check(d.c, les_solve_jacobi(d.c, dt, rho, 100, 1e-6, &sweeps), "les_solve_jacobi");   // :134, :165
@@ -238,7 +256,7 @@ void solve_pressure_GS(Field& f, const Mesh& m, double dt, double rho, int maxIt
 {
     std::lock_guard<std::mutex> lk(g_mu);
     Dev& d = dev_for(m);
-    up(d, LES_U, f.u); up(d, LES_V, f.v); up(d, LES_W, f.w); up(d, LES_P, f.p);
+    ups(d, {{LES_U, &f.u}, {LES_V, &f.v}, {LES_W, &f.w}, {LES_P, &f.p}});
     up_mask(d, f);
     int sweeps = 0;
     check(d.c, les_solve_gs(d.c, dt, rho, maxIter, 1.7, 1e-6, &sweeps), "les_solve_gs");   // :195, :240
@@ -250,7 +268,7 @@ void calculate_divergence(Vector& rhs, const Field& f, const Mesh& m, double dt,
 {
     std::lock_guard<std::mutex> lk(g_mu);
     Dev& d = dev_for(m);
-    up(d, LES_U_NEW, f.u_new); up(d, LES_V_NEW, f.v_new); up(d, LES_W_NEW, f.w_new);
+    ups(d, {{LES_U_NEW, &f.u_new}, {LES_V_NEW, &f.v_new}, {LES_W_NEW, &f.w_new}});
     up_mask(d, f);
     check(d.c, les_divergence(d.c, dt, rho), "les_divergence");
     down(d, LES_P_RHS, rhs);

@@ -191,6 +191,19 @@ class Context:
     def download_ptr(self, slot, ptr):
         self._chk(self.lib.les_download(self.h, SLOTS.get(slot, slot), C.cast(ptr, _dp)))
 
+    def upload_many_ptr(self, slot_ptrs):
+        """{slot: host pointer} in one call (one synchronisation)."""
+        n = len(slot_ptrs)
+        sl = (C.c_int * n)(*[SLOTS.get(k, k) for k in slot_ptrs])
+        ps = (_dp * n)(*[C.cast(p, _dp) for p in slot_ptrs.values()])
+        self._chk(self.lib.les_upload_many(self.h, n, sl, ps))
+
+    def download_many_ptr(self, slot_ptrs):
+        n = len(slot_ptrs)
+        sl = (C.c_int * n)(*[SLOTS.get(k, k) for k in slot_ptrs])
+        ps = (_dp * n)(*[C.cast(p, _dp) for p in slot_ptrs.values()])
+        self._chk(self.lib.les_download_many(self.h, n, sl, ps))
+
     def upload_mask(self, m):
         m = _arr(m, np.uint8)
         assert m.size == self.n

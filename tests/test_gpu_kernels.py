@@ -279,3 +279,22 @@ def test_big_pressure_ops(oracle_lib, big):
         p = big["p"].copy()
         oracle_lib.solve_jacobi(m, 1e-4, 1.2, big["u"], big["v"], big["w"], p, s, 9, 1e-6)
         assert same(c.download("p"), p)
+
+
+def test_upload_download_many_round_trip():
+    """Several slots per call (one synchronisation) move the same bytes as
+    one call per slot, and reject a bad slot before copying anything."""
+    shape = (9, 7, 5)
+    n = int(np.prod(shape))
+    rng = np.random.default_rng(3)
+    with G.Context(G.Mesh(*shape, 0.1, 0.2, 0.3)) as c:
+        src = {k: rng.standard_normal(n) for k in ("u", "v", "w", "p", "nu_t")}
+        c.upload_many_ptr({k: v.ctypes.data for k, v in src.items()})
+        for k, v in src.items():
+            assert same(c.download(k), v), k
+        out = {k: np.empty(n) for k in src}
+        c.download_many_ptr({k: v.ctypes.data for k, v in out.items()})
+        for k in src:
+            assert same(out[k], src[k]), k
+        with pytest.raises(RuntimeError):
+            c.upload_many_ptr({99: src["u"].ctypes.data})
