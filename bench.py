@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--adj-steps", type=int, default=50, help="adjoint workload: forward steps")
     ap.add_argument("--fd-step", type=float, default=1e-6, help="adjoint workload: finite-difference step")
     ap.add_argument("--batch", type=int, default=64, help="cases of the batch workload")
+    ap.add_argument("--ens-batched", type=int, default=1,
+                    help="batch workload: 1 the cases' solves in shared kernels, 0 one graph branch per case")
     ap.add_argument("--tune", type=int, default=1,
                     help="run the strip-shape autotuner before warm-up (column passes, built-in rows/chunks)")
     ap.add_argument("--precond", default="cheb", choices=("cheb", "jacobi", "ic"))
@@ -291,8 +293,10 @@ def run_reference(args):
 def run_batch(args):
     """Ensemble workload: `--batch` ragged cases (dims from {32..96}, random
     cube obstacle, Cs from [0.1, 0.2], inflow noise 0.02), mixed-precision
-    Chebyshev(4)-PCG, every step one CUDA graph launch for all cases; strip
-    shapes and chunk lengths from the ensemble autotuner."""
+    Chebyshev(4)-PCG, every step one CUDA graph launch for all cases.  By
+    default the cases' solves share kernels (one launch per inner pass over
+    all cases); with --ens-batched 0 each case is its own graph branch, with
+    strip shapes and chunk lengths from the ensemble autotuner."""
     import torch
     import les_cases
     import les_gb300 as G
@@ -309,6 +313,7 @@ def run_batch(args):
     specs = [all_specs[i] for i in shard_cases([int(np.prod(s["shape"])) for s in all_specs], rank, world)]
     meshes = [G.Mesh(*s["shape"], s["h"], s["h"], s["h"]) for s in specs]
     ens = G.Ensemble(meshes)
+    ens.set_batched(args.ens_batched)
     prm = []
     for c, s in zip(ens.cases, specs):
         shape = s["shape"]
@@ -331,7 +336,7 @@ def run_batch(args):
                                                 inner_rtol=args.inner_rtol)))
     cells = sum(int(np.prod(s["shape"])) for s in specs)
     t0 = time.perf_counter()
-    tune_us = ens.autotune(prm[0].pcg) if args.tune else None
+    tune_us = ens.autotune(prm[0].pcg) if args.tune and not args.ens_batched else None
     tune_s = time.perf_counter() - t0
     t0 = time.perf_counter()
     for _ in range(args.warmup):
@@ -373,6 +378,7 @@ def run_batch(args):
                        "timing": "host wall clock around each step's launch + stats sync, max over ranks",
                        "l2": "inputs (~%.1f GB) larger than L2" % (cells * 120 / 1e9),
                        "pdl": 0 if args.pdl is None else args.pdl, "phys32": args.phys32,
+                       "form": "batched solves" if args.ens_batched else "one branch per case",
                        "autotune_us_per_iteration": tune_us, "autotune_s": tune_s,
                        "first_steps_with_capture_s": warm_s},
             "gpu_launches": launches, "iters_inner_mean": statistics.mean(iters), "rel_residual_max": worst,

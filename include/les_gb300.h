@@ -333,6 +333,12 @@ les_status les_autotune(les_ctx* ctx, const les_pcg_opts* opts, double share, do
  * candidate concurrently, as in a step), choosing one setting per case
  * from the total time. */
 les_status les_ensemble_autotune(les_ensemble* ens, const les_pcg_opts* opts, double* best_us);
+/* 1 (default): the cases' mixed-precision solves run batched -- every inner
+ * pass, defect and update is one kernel over all cases, and the solver loops
+ * run while any case iterates (used when all cases run the register-column
+ * passes with one preconditioner; otherwise, and with 0, each case's step is
+ * its own branch of the step graph). */
+les_status les_ensemble_set_batched(les_ensemble* ens, int on);
 
 /* ---- options (no reference counterpart) --------------------------------- */
 typedef enum les_option {

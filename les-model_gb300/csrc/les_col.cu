@@ -103,17 +103,18 @@ __device__ __forceinline__ int row_off(const Geo& g, const StripPos& s, int P, i
 }
 
 // ---- pass A -----------------------------------------------------------------
+// blk / nblk: this block among the blocks of the pass (one case's blocks in
+// a batched launch)
 template <int TJ, bool FIRST>
-__global__ void __launch_bounds__(CT, TJ == 8 ? 4 : 2) k_col_a(Geo g, ColMap m, Coef k, const float* __restrict__ z,
-                                                             const float* __restrict__ pold, float* __restrict__ pnew,
-                                                             float* __restrict__ q, float* __restrict__ e,
-                                                             double* partials, unsigned* counter, SolverState* st,
-                                                             int pslot)
+__device__ __forceinline__ void col_a(const Geo& g, const ColMap& m, const Coef& k, const float* __restrict__ z,
+                                      const float* __restrict__ pold, float* __restrict__ pnew, float* __restrict__ q,
+                                      float* __restrict__ e, double* partials, unsigned* counter, SolverState* st,
+                                      int pslot, int blk, int nblk)
 {
     constexpr int H = TJ + 2;
     __shared__ double sm[32];
     const int lane = threadIdx.x & 31;
-    const int item = blockIdx.x * CWPB + (threadIdx.x >> 5);
+    const int item = blk * CWPB + (threadIdx.x >> 5);
     const StripPos s = strip_pos<1, TJ>(g, m, item, lane);   // from the arguments only
     dep_wait();
     if (st->done) return;
@@ -199,7 +200,7 @@ __global__ void __launch_bounds__(CT, TJ == 8 ? 4 : 2) k_col_a(Geo g, ColMap m, 
     }
     dep_signal();
     double v[1] = {acc_value(acc)};
-    if (last_block_sum<1>(v, partials, counter, sm)) {
+    if (last_block_sum<1>(v, partials, counter, sm, blk, nblk)) {
         if (threadIdx.x == 0) {
             st->alpha = st->rho / v[0];
             st->buf = pslot;   // buffer holding this iteration's p
@@ -207,15 +208,26 @@ __global__ void __launch_bounds__(CT, TJ == 8 ? 4 : 2) k_col_a(Geo g, ColMap m, 
     }
 }
 
+template <int TJ, bool FIRST>
+__global__ void __launch_bounds__(CT, TJ == 8 ? 4 : 2) k_col_a(Geo g, ColMap m, Coef k, const float* __restrict__ z,
+                                                             const float* __restrict__ pold, float* __restrict__ pnew,
+                                                             float* __restrict__ q, float* __restrict__ e,
+                                                             double* partials, unsigned* counter, SolverState* st,
+                                                             int pslot)
+{
+    col_a<TJ, FIRST>(g, m, k, z, pold, pnew, q, e, partials, counter, st, pslot, blockIdx.x, gridDim.x);
+}
+
 // ---- pass B -----------------------------------------------------------------
 // Grid sums of ||r'||^2 and r'.z; the last block updates the inner state:
 // the first pass sets rho, later ones the convergence test, beta and rho.
 template <bool FIRST>
 __device__ __forceinline__ void pass_b_finish(const Acc& arr, const Acc& arz, double* partials, unsigned* counter,
-                                              double* sm, SolverState* st, SolverState* outer, int total_cap)
+                                              double* sm, SolverState* st, SolverState* outer, int total_cap,
+                                              int blk, int nblk)
 {
     double v[2] = {acc_value(arr), acc_value(arz)};
-    if (last_block_sum<2>(v, partials, counter, sm)) {
+    if (last_block_sum<2>(v, partials, counter, sm, blk, nblk)) {
         if (threadIdx.x == 0) {
             if (FIRST) {
                 st->rho = v[1];
@@ -237,17 +249,17 @@ __device__ __forceinline__ void pass_b_finish(const Acc& arr, const Acc& arz, do
 }
 
 template <int S, int TJ, bool FIRST>
-__global__ void __launch_bounds__(CT, (TJ == 4 && S <= 3) ? 3 : 2) k_col_b(Geo g, ColMap m, Coef k, ChebF cf, float inv_c0,
-                                               const float* __restrict__ r_in, float* __restrict__ r_out,
-                                               const float* __restrict__ q, float* __restrict__ z_out,
-                                               double* partials, unsigned* counter, SolverState* st,
-                                               SolverState* outer, int total_cap)
+__device__ __forceinline__ void col_b(const Geo& g, const ColMap& m, const Coef& k, const ChebF& cf, float inv_c0,
+                                      const float* __restrict__ r_in, float* __restrict__ r_out,
+                                      const float* __restrict__ q, float* __restrict__ z_out, double* partials,
+                                      unsigned* counter, SolverState* st, SolverState* outer, int total_cap, int blk,
+                                      int nblk)
 {
     constexpr int H = TJ + 2 * S;
     constexpr int NL = S > 1 ? S - 1 : 1;   // stored levels z_1 .. z_{S-1}
     __shared__ double sm[64];
     const int lane = threadIdx.x & 31;
-    const int item = blockIdx.x * CWPB + (threadIdx.x >> 5);
+    const int item = blk * CWPB + (threadIdx.x >> 5);
     const StripPos s = strip_pos<S, TJ>(g, m, item, lane);   // from the arguments only
     dep_wait();
     if (st->done) return;
@@ -388,7 +400,18 @@ __global__ void __launch_bounds__(CT, (TJ == 4 && S <= 3) ? 3 : 2) k_col_b(Geo g
         }
     }
     dep_signal();
-    pass_b_finish<FIRST>(arr, arz, partials, counter, sm, st, outer, total_cap);
+    pass_b_finish<FIRST>(arr, arz, partials, counter, sm, st, outer, total_cap, blk, nblk);
+}
+
+template <int S, int TJ, bool FIRST>
+__global__ void __launch_bounds__(CT, (TJ == 4 && S <= 3) ? 3 : 2) k_col_b(Geo g, ColMap m, Coef k, ChebF cf, float inv_c0,
+                                               const float* __restrict__ r_in, float* __restrict__ r_out,
+                                               const float* __restrict__ q, float* __restrict__ z_out,
+                                               double* partials, unsigned* counter, SolverState* st,
+                                               SolverState* outer, int total_cap)
+{
+    col_b<S, TJ, FIRST>(g, m, k, cf, inv_c0, r_in, r_out, q, z_out, partials, counter, st, outer, total_cap, blockIdx.x,
+                        gridDim.x);
 }
 
 // x += e + alpha p_last (FP64 solution, FP32 correction)
@@ -400,6 +423,49 @@ __global__ void k_x_update(Geo g, double* __restrict__ x, const float* __restric
     const float a = (float)in->alpha;
     const float* p = in->buf ? p1 : p0;
     x[t] = __dadd_rn(x[t], (double)fmaf(a, p[t], e[t]));
+}
+
+// ---- batched over the cases of an ensemble ------------------------------------
+// Each block finds its case from the prefix of block starts and runs the
+// single-case body on that case's block range; blocks of a case whose inner
+// solve is done leave at once.  (Pass A runs 3 blocks per SM here: the case's
+// fields take registers that the single-case kernel reads from its
+// parameters, and 4 blocks would spill.)
+template <int TJ, bool FIRST>
+__global__ void __launch_bounds__(CT, TJ == 8 ? 3 : 2) k_col_a_batch(const BatchCase* __restrict__ cs,
+                                                                   const int* __restrict__ pre, int n, int pc)
+{
+    const int c = batch_case(pre, n, blockIdx.x);
+    const BatchCase& C = cs[c];
+    const int b0 = __ldg(pre + c), nb = __ldg(pre + c + 1) - b0;
+    col_a<TJ, FIRST>(C.g, C.ma, Coef{C.c0, C.x1, C.y1, C.z1}, C.z, pc ? C.p1 : C.p0, pc ? C.p0 : C.p1, C.q, C.e,
+                     C.partials, C.counters + 15, C.in, pc ^ 1, blockIdx.x - b0, nb);
+}
+
+template <int S, int TJ, bool FIRST>
+__global__ void __launch_bounds__(CT, (TJ == 4 && S <= 3) ? 3 : 2) k_col_b_batch(const BatchCase* __restrict__ cs,
+                                                                               const int* __restrict__ pre, int n,
+                                                                               int rin)
+{
+    const int c = batch_case(pre, n, blockIdx.x);
+    const BatchCase& C = cs[c];
+    const int b0 = __ldg(pre + c), nb = __ldg(pre + c + 1) - b0;
+    col_b<S, TJ, FIRST>(C.g, C.mb, Coef{C.c0, C.x1, C.y1, C.z1}, C.cf, C.inv_c0, rin ? C.r1 : C.r0,
+                        rin ? C.r0 : C.r1, C.q, C.z, C.partials, C.counters + 14, C.in, C.out, C.cap, blockIdx.x - b0,
+                        nb);
+}
+
+// x += e + alpha p_last for the cases in their correction round
+__global__ void k_x_update_batch(const BatchCase* __restrict__ cs, const int* __restrict__ pre, int n)
+{
+    const int c = batch_case(pre, n, blockIdx.x);
+    const BatchCase& C = cs[c];
+    if (!C.act) return;
+    const int t = (blockIdx.x - __ldg(pre + c)) * blockDim.x + threadIdx.x;
+    if (t >= C.g.n) return;
+    const float a = (float)C.in->alpha;
+    const float* p = C.in->buf ? C.p1 : C.p0;
+    C.x[t] = __dadd_rn(C.x[t], (double)fmaf(a, p[t], C.e[t]));
 }
 
 // ---- launch plumbing ----------------------------------------------------------
@@ -520,6 +586,64 @@ les_status col_pass_b(les_ctx* c, const ColPlan& P, bool first, int rin)
     launch_pdl(c, PROF_IN_CHEB, pick_b(P.S, P.mb.tj, first), P.blocks_b, CT, c->g, P.mb, coef_of(P), P.cf, P.inv_c0,
              (const float*)r[rin], r[rin ^ 1], (const float*)q, z, c->partials, c->counters + 14, P.in, P.out, P.cap);
     return check_launch(c, "column pass B");
+}
+
+// ---- batched passes ------------------------------------------------------------
+using KAB = void (*)(const BatchCase*, const int*, int, int);
+
+static KAB pick_a_batch(bool first) { return first ? k_col_a_batch<8, true> : k_col_a_batch<8, false>; }
+
+static KAB pick_b_batch(int S, bool first)
+{
+#define LES_BB(s, t) return first ? k_col_b_batch<s, t, true> : k_col_b_batch<s, t, false>
+    switch (S) {
+    case 0: LES_BB(0, 16);
+    case 1: LES_BB(1, 8);
+    case 2: LES_BB(2, 8);
+    case 3: LES_BB(3, 8);
+    case 4: LES_BB(4, 4);
+    case 5: LES_BB(5, 4);
+    default: LES_BB(6, 4);
+    }
+#undef LES_BB
+}
+
+int col_batch_tj_b(int S) { return default_tj_b(S); }
+
+ColMap col_batch_map(les_ctx* c, int pass, int S, int chunk_planes)
+{
+    if (pass == 0) return col_map(c, (const void*)pick_a_batch(false), 1, 8, chunk_planes);
+    return col_map(c, (const void*)pick_b_batch(S, false), S, default_tj_b(S), chunk_planes);
+}
+
+int col_batch_resident_warps(int pass, int S)
+{
+    int occ = 1, dev = 0, sms = 1;
+    const void* fn = pass == 0 ? (const void*)pick_a_batch(false) : (const void*)pick_b_batch(S, false);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, CT, 0);
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return (occ < 1 ? 1 : occ) * CWPB * sms;
+}
+
+les_status col_batch_pass_a(cudaStream_t s, bool first, int pc, const BatchCase* cs, const int* pre, int n,
+                            int blocks)
+{
+    pick_a_batch(first)<<<blocks, CT, 0, s>>>(cs, pre, n, pc);
+    return cudaPeekAtLastError() == cudaSuccess ? LES_OK : LES_CUDA_ERROR;
+}
+
+les_status col_batch_pass_b(cudaStream_t s, int S, bool first, int rin, const BatchCase* cs, const int* pre, int n,
+                            int blocks)
+{
+    pick_b_batch(S, first)<<<blocks, CT, 0, s>>>(cs, pre, n, rin);
+    return cudaPeekAtLastError() == cudaSuccess ? LES_OK : LES_CUDA_ERROR;
+}
+
+les_status col_batch_x_update(cudaStream_t s, const BatchCase* cs, const int* pre, int n, int blocks)
+{
+    k_x_update_batch<<<blocks, 256, 0, s>>>(cs, pre, n);
+    return cudaPeekAtLastError() == cudaSuccess ? LES_OK : LES_CUDA_ERROR;
 }
 
 les_status col_x_update(les_ctx* c)

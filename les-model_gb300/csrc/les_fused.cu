@@ -954,46 +954,8 @@ __global__ void k_cond_outer(const SolverState* out, cudaGraphConditionalHandle 
 template <class Entry, class Body>
 static les_status capture_while(les_ctx* c, Entry entry, Body body)
 {
-    cudaStreamCaptureStatus cs;
-    cudaGraph_t g = nullptr;
-    const cudaGraphNode_t* deps = nullptr;
-    size_t ndeps = 0;
-    les_status st = check_cuda(c, cudaStreamGetCaptureInfo(c->stream, &cs, nullptr, &g, &deps, nullptr, &ndeps),
-                               "capture info");
-    if (st) return st;
-    if (cs != cudaStreamCaptureStatusActive) return fail(c, LES_BAD_ARG, "internal: not capturing");
-    cudaGraphConditionalHandle h;
-    st = check_cuda(c, cudaGraphConditionalHandleCreate(&h, g, 0, 0), "conditional handle");
-    if (st) return st;
-    if ((st = entry(h))) return st;
-    st = check_cuda(c, cudaStreamGetCaptureInfo(c->stream, &cs, nullptr, &g, &deps, nullptr, &ndeps), "capture info");
-    if (st) return st;
-    cudaGraphNodeParams np = {};
-    np.type = cudaGraphNodeTypeConditional;
-    np.conditional.handle = h;
-    np.conditional.type = cudaGraphCondTypeWhile;
-    np.conditional.size = 1;
-    cudaGraphNode_t node;
-    st = check_cuda(c, cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &np), "conditional node");
-    if (st) return st;
-    cudaGraph_t bodyg = np.conditional.phGraph_out[0];
-    cudaStream_t outer = c->stream, inner = nullptr;
-    st = check_cuda(c, cudaStreamCreateWithFlags(&inner, cudaStreamNonBlocking), "body stream");
-    if (st) return st;
-    st = check_cuda(c, cudaStreamBeginCaptureToGraph(inner, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed),
-                    "body capture");
-    if (!st) {
-        c->stream = inner;
-        st = body(h);
-        c->stream = outer;
-        cudaGraph_t got = nullptr;
-        les_status st2 = check_cuda(c, cudaStreamEndCapture(inner, &got), "end body capture");
-        if (!st) st = st2;
-    }
-    cudaStreamDestroy(inner);
-    if (st) return st;
-    return check_cuda(c, cudaStreamUpdateCaptureDependencies(outer, &node, nullptr, 1, cudaStreamSetCaptureDependencies),
-                      "resume capture");
+    return capture_while_on(&c->stream, [c](cudaError_t r, const char* what) { return check_cuda(c, r, what); },
+                            entry, body);
 }
 
 // Emits the mixed solve of les_mixed.cu (outer FP64 defect correction, inner

@@ -160,13 +160,14 @@ __device__ __forceinline__ int block_count() { return gridDim.x * gridDim.y * gr
 // Two-stage deterministic sum: each block stores its partial; the block that
 // arrives last sums all partials in block order.  Returns true in every
 // thread of the last block, with the totals valid in its thread 0.
+// (bid, nb): this block's index among the nb blocks that share the
+// reduction -- the whole grid, or one case's blocks of a batched launch.
 template <int NV>
-__device__ bool last_block_sum(double (&v)[NV], double* partials, unsigned* counter, double* smem)
+__device__ bool last_block_sum(double (&v)[NV], double* partials, unsigned* counter, double* smem, int bid, int nb)
 {
     __shared__ int am_last;
     const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
     const int nthr = blockDim.x * blockDim.y * blockDim.z;
-    const int nb = block_count(), bid = block_linear_id();
     block_sum<NV>(v, smem);
     if (tid == 0) {
 #pragma unroll
@@ -191,6 +192,12 @@ __device__ bool last_block_sum(double (&v)[NV], double* partials, unsigned* coun
         *counter = 0u;
     }
     return true;
+}
+
+template <int NV>
+__device__ bool last_block_sum(double (&v)[NV], double* partials, unsigned* counter, double* smem)
+{
+    return last_block_sum<NV>(v, partials, counter, smem, block_linear_id(), block_count());
 }
 
 // ---- device-resident solver state -----------------------------------------
@@ -397,6 +404,10 @@ les_status ensure_work32(les_ctx* c);
 // graph-captured time steps (les_step.cu)
 bool graph_eligible(const les_ctx* c, const les_step_params* prm);
 les_status emit_step(les_ctx* c, const les_step_params* prm);   // into the capture on c->stream
+// the step before the pressure solve (with its first FP64 defect when
+// outer_start) and after it
+les_status emit_step_pre(les_ctx* c, const les_step_params* prm, bool outer_start);
+les_status emit_step_post(les_ctx* c, const les_step_params* prm);
 void swap_velocity(les_ctx* c);
 unsigned long long graph_step_stats(les_ctx* c, const les_step_params* prm, unsigned long long captured,
                                     les_step_stats* stats);

@@ -70,23 +70,26 @@ inline dim3 resid_grid(const Geo& g)
 
 // Outer residual: r = b - A x in FP64, its FP32 copy for the inner solve, and
 // ||r||^2 in FP64.  Sets the outer state done once ||r|| < tol.
-__global__ void k_outer_resid(Geo g, StencilView A, const double* __restrict__ x, const double* __restrict__ b,
-                              float* __restrict__ r32, double* partials, unsigned* counter, SolverState* st,
-                              int outer)
+// (bx, by, bz): block coordinates in the grid of resid_grid(g); (lb, nb):
+// this block among the blocks of the reduction
+__device__ __forceinline__ void outer_resid(const Geo& g, const StencilView& A, const double* __restrict__ x,
+                                            const double* __restrict__ b, float* __restrict__ r32, double* partials,
+                                            unsigned* counter, SolverState* st, int outer, int bx, int by, int bz,
+                                            int lb, int nb)
 {
     __shared__ double sm[32];
-    int i, j, k;
+    const int k = bx * TBK + threadIdx.x, j = by * TBJ + threadIdx.y;
     double rr[1] = {0.0};
-    if (cell_coords(g, i, j, k)) {   // blockIdx.z: a group of RES_PLANES planes
-        const int i0 = i * RES_PLANES, i1 = min(g.nx, i0 + RES_PLANES);
-        for (i = i0; i < i1; ++i) {
+    if (k < g.nz && j < g.ny) {   // bz: a group of RES_PLANES planes
+        const int i0 = bz * RES_PLANES, i1 = min(g.nx, i0 + RES_PLANES);
+        for (int i = i0; i < i1; ++i) {
             const int id = i * g.si + j * g.sj + k;
             const double r = b[id] - row64(A, x, g, i, j, k, id);
             r32[id] = d2f_bits(r);
             rr[0] = fma(r, r, rr[0]);
         }
     }
-    if (last_block_sum<1>(rr, partials, counter, sm)) {
+    if (last_block_sum<1>(rr, partials, counter, sm, lb, nb)) {
         if (threadIdx.x == 0 && threadIdx.y == 0) {
             double e = sqrt(rr[0]);
             st->err = e;
@@ -96,6 +99,27 @@ __global__ void k_outer_resid(Geo g, StencilView A, const double* __restrict__ x
             else if (!isfinite(e)) { st->done = 1; st->status = LES_NONFINITE; }
         }
     }
+}
+
+__global__ void k_outer_resid(Geo g, StencilView A, const double* __restrict__ x, const double* __restrict__ b,
+                              float* __restrict__ r32, double* partials, unsigned* counter, SolverState* st,
+                              int outer)
+{
+    outer_resid(g, A, x, b, r32, partials, counter, st, outer, blockIdx.x, blockIdx.y, blockIdx.z, block_linear_id(),
+                block_count());
+}
+
+// The defects of the cases in their correction round of a batched ensemble
+// solve (each counts the round on the device).
+__global__ void k_outer_resid_batch(const BatchCase* __restrict__ cs, const int* __restrict__ pre, int n)
+{
+    const int c = batch_case(pre, n, blockIdx.x);
+    const BatchCase& C = cs[c];
+    if (!C.act) return;
+    const int b0 = __ldg(pre + c), nb = __ldg(pre + c + 1) - b0, lb = blockIdx.x - b0;
+    const int gx = (C.g.nz + TBK - 1) / TBK, gy = (C.g.ny + TBJ - 1) / TBJ;
+    outer_resid(C.g, C.A, C.x, C.b, C.r0, C.partials, C.counters + 8, C.out, -1, lb % gx, (lb / gx) % gy,
+                lb / (gx * gy), lb, nb);
 }
 
 __global__ void k_x_add(Geo g, double* __restrict__ x, const float* __restrict__ e)
@@ -487,6 +511,19 @@ les_status pcg_mixed_impl(les_ctx* c, const les_pcg_opts* o, les_pcg_result* res
 }
 
 ViewF view32_of(les_ctx* c) { return view32(c); }
+StencilView stencil_view_of(les_ctx* c) { return stencil_view(c); }
+
+int batch_resid_blocks(const Geo& g)
+{
+    const dim3 r = resid_grid(g);
+    return (int)(r.x * r.y * r.z);
+}
+
+les_status batch_outer_resid(cudaStream_t s, const BatchCase* cs, const int* pre, int n, int blocks)
+{
+    k_outer_resid_batch<<<blocks, cell_block(), 0, s>>>(cs, pre, n);
+    return cudaPeekAtLastError() == cudaSuccess ? LES_OK : LES_CUDA_ERROR;
+}
 
 // Launch helpers for the graph-captured mixed solve (les_fused.cu): the same
 // kernels as pcg_mixed_impl, with the outer count kept on the device.

@@ -132,6 +132,105 @@ les_status col_pass_b(les_ctx* c, const ColPlan& P, bool first, int rin);
 les_status col_x_update(les_ctx* c);
 les_status inner_solve_fused(les_ctx* c, const les_pcg_opts* o, ViewF A, SolverState* in, SolverState* out,
                              int inner_cap);
+// ---- batched ensemble solve (les_ensemble.cu) ------------------------------
+// One case of a mixed-precision solve that advances together with the other
+// cases of an ensemble: each batched kernel covers every case, its blocks
+// split into consecutive per-case ranges (prefix arrays of block starts), and
+// each block works on its own case only.  Lives in device memory.
+struct BatchCase {
+    Geo g;
+    ColMap ma, mb;                 // column-pass work splits
+    float c0, x1, y1, z1;          // plane-uniform FP32 coefficients
+    ChebF cf;
+    float inv_c0;
+    float *r0, *r1, *z, *p0, *p1, *q, *e;   // FP32 inner vectors
+    double* x;                     // FP64 solution (the pressure slot)
+    const double* b;               // FP64 right-hand side
+    StencilView A;                 // FP64 matrix for the defect
+    double* partials;
+    unsigned* counters;
+    SolverState* out;
+    SolverState* in;
+    double inner_rtol;
+    int cap, inner_cap, max_outer; // total inner iterations, per correction, corrections
+    int act;                       // the current correction round runs for this case
+};
+
+// block -> case of a batched grid (pre: n + 1 block starts, ascending)
+__device__ __forceinline__ int batch_case(const int* pre, int n, int block)
+{
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(pre + mid) <= block) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// column passes over all cases (S levels; rows as in the single-case default)
+int col_batch_tj_b(int S);
+ColMap col_batch_map(les_ctx* c, int pass, int S, int chunk_planes);   // pass 0: A, 1: B
+int col_batch_resident_warps(int pass, int S);
+les_status col_batch_pass_a(cudaStream_t s, bool first, int pc, const BatchCase* cs, const int* pre, int n,
+                            int blocks);
+les_status col_batch_pass_b(cudaStream_t s, int S, bool first, int rin, const BatchCase* cs, const int* pre, int n,
+                            int blocks);
+les_status col_batch_x_update(cudaStream_t s, const BatchCase* cs, const int* pre, int n, int blocks);
+// the FP64 defect of every case still in its correction round (les_mixed.cu)
+les_status batch_outer_resid(cudaStream_t s, const BatchCase* cs, const int* pre, int n, int blocks);
+int batch_resid_blocks(const Geo& g);
+StencilView stencil_view_of(les_ctx* c);
+
+// Adds a `while` loop at the current capture point of *stream: creates the
+// loop's condition handle, captures `entry(h)` (a kernel that sets the
+// condition from the solver state, so the loop can be skipped and is
+// re-armed each time an enclosing loop comes back to it), adds the
+// conditional node, captures its body with `body(h)` -- *stream points to the
+// body's capture stream meanwhile -- which must end by setting the condition
+// again, and resumes the capture after the node.  check(err, what) turns a
+// CUDA error into a status.
+template <class Check, class Entry, class Body>
+les_status capture_while_on(cudaStream_t* stream, Check check, Entry entry, Body body)
+{
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    les_status st = check(cudaStreamGetCaptureInfo(*stream, &cs, nullptr, &g, &deps, nullptr, &ndeps), "capture info");
+    if (st) return st;
+    if (cs != cudaStreamCaptureStatusActive) return LES_BAD_ARG;
+    cudaGraphConditionalHandle h;
+    if ((st = check(cudaGraphConditionalHandleCreate(&h, g, 0, 0), "conditional handle"))) return st;
+    if ((st = entry(h))) return st;
+    if ((st = check(cudaStreamGetCaptureInfo(*stream, &cs, nullptr, &g, &deps, nullptr, &ndeps), "capture info")))
+        return st;
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    if ((st = check(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &np), "conditional node"))) return st;
+    cudaGraph_t bodyg = np.conditional.phGraph_out[0];
+    cudaStream_t outer = *stream, inner = nullptr;
+    if ((st = check(cudaStreamCreateWithFlags(&inner, cudaStreamNonBlocking), "body stream"))) return st;
+    st = check(cudaStreamBeginCaptureToGraph(inner, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed),
+               "body capture");
+    if (!st) {
+        *stream = inner;
+        st = body(h);
+        *stream = outer;
+        cudaGraph_t got = nullptr;
+        les_status st2 = check(cudaStreamEndCapture(inner, &got), "end body capture");
+        if (!st) st = st2;
+    }
+    cudaStreamDestroy(inner);
+    if (st) return st;
+    return check(cudaStreamUpdateCaptureDependencies(outer, &node, nullptr, 1, cudaStreamSetCaptureDependencies),
+                 "resume capture");
+}
+
 // graph capture of the whole mixed solve (fused inner iteration)
 les_status emit_outer_start(les_ctx* c, const les_pcg_opts* o, int keep_tol);
 les_status emit_inner_start(les_ctx* c, const les_pcg_opts* o, int inner_cap);

@@ -112,23 +112,43 @@ static bool graph_matches(const les_ctx* c, const StepGraph* s, const les_step_p
            std::memcmp(&s->prm, prm, sizeof *prm) == 0 && std::memcmp(s->slots, c->slot, sizeof s->slots) == 0;
 }
 
-// One step (src/main.cpp:115-144) into the capture in progress on c->stream.
-les_status les::emit_step(les_ctx* c, const les_step_params* prm)
+// dt of a captured step: fixed, or read by the kernels from the CFL reduction
+static double step_dt(les_ctx* c, const les_step_params* prm, const double** dtp)
+{
+    *dtp = prm->dt_fixed > 0 ? nullptr : &c->state[0].scal[0];   // nothing else in the step writes it
+    return prm->dt_fixed > 0 ? prm->dt_fixed : 1.0;                // (1.0 unused: the kernels read *dtp)
+}
+
+// One step (src/main.cpp:115-144) into the capture in progress on c->stream,
+// in three parts: up to the pressure solve's first defect, the solve, and
+// the projection (an ensemble solves its cases together between the parts).
+les_status les::emit_step_pre(les_ctx* c, const les_step_params* prm, bool outer_start)
 {
     les_status st;
-    double dt = prm->dt_fixed;
-    const double* dtp = nullptr;
-    if (!(dt > 0)) {
-        if ((st = adaptive_dt_dev(c, prm->nu, prm->cfl_conv, prm->cfl_visc, prm->dt_max))) return st;
-        dtp = &c->state[0].scal[0];   // nothing else in the step writes it
-        dt = 1.0;                     // unused: the kernels read *dtp
-    }
+    const double* dtp;
+    const double dt = step_dt(c, prm, &dtp);
+    if (dtp && (st = adaptive_dt_dev(c, prm->nu, prm->cfl_conv, prm->cfl_visc, prm->dt_max))) return st;
     if ((st = physics_dev(c, prm, dt, dtp))) return st;
     if ((st = velocity_bcs_dev(c))) return st;
     if ((st = div_b_dev(c, dt, prm->rho, prm->rel_tol, dtp))) return st;
-    if ((st = capture_mixed_fused(c, &prm->pcg, view32_of(c), prm->rel_tol > 0 ? 1 : 0))) return st;
+    return outer_start ? emit_outer_start(c, &prm->pcg, prm->rel_tol > 0 ? 1 : 0) : LES_OK;
+}
+
+les_status les::emit_step_post(les_ctx* c, const les_step_params* prm)
+{
+    les_status st;
+    const double* dtp;
+    const double dt = step_dt(c, prm, &dtp);
     if ((st = correct_dev(c, dt, prm->rho, dtp))) return st;
     return velocity_bcs_dev(c);
+}
+
+les_status les::emit_step(les_ctx* c, const les_step_params* prm)
+{
+    les_status st;
+    if ((st = emit_step_pre(c, prm, false))) return st;
+    if ((st = capture_mixed_fused(c, &prm->pcg, view32_of(c), prm->rel_tol > 0 ? 1 : 0))) return st;
+    return emit_step_post(c, prm);
 }
 
 static les_status step_graph(les_ctx* c, const les_step_params* prm, les_step_stats* stats)

@@ -441,6 +441,11 @@ class Ensemble:
         self._chk(self.lib.les_ensemble_autotune(self.h, C.byref(opts), C.byref(us)))
         return us.value
 
+    def set_batched(self, on):
+        """1: the cases' solves run batched (one kernel per pass over all
+        cases); 0: one graph branch per case."""
+        self._chk(self.lib.les_ensemble_set_batched(self.h, int(on)))
+
     def close(self):
         if self.h:
             for c in self.cases:
