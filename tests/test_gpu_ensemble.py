@@ -148,3 +148,18 @@ def test_batched_and_branch_forms_switch():
         st = ens.step(prm)
         for x in st:
             assert x.status == G.OK and x.residual < 1e-8 * x.b_norm
+
+
+def test_batched_ensemble_case_hitting_its_cap():
+    """A case whose iteration cap is too small ends NOT_CONVERGED after its
+    cap while the other cases of the shared loops converge (the loops run
+    while any case iterates, and every pass advances each unfinished case)."""
+    specs = _specs(3, 41)
+    with G.Ensemble([_mesh(s) for s in specs]) as ens:
+        prm = [_params(s, _setup(c, s)) for c, s in zip(ens.cases, specs)]
+        prm[1].pcg.max_iter = 30            # total inner iterations of the solve
+        prm[1].pcg.inner_max_iter = 30
+        st = ens.step(prm)
+    assert st[1].status == G.NOT_CONVERGED and st[1].iters <= 31, (st[1].status, st[1].iters)
+    for i in (0, 2):
+        assert st[i].status == G.OK and st[i].residual < 1e-8 * st[i].b_norm, (i, st[i].status)
