@@ -1,5 +1,8 @@
-// les_mixed.cuh -- FP32 view of the pressure matrix for the mixed-precision
-// inner solve (les_mixed.cu, les_fused.cu).
+// les_mixed.cuh -- shared pieces of the mixed-precision solve: the FP32 view
+// of the pressure matrix, the Chebyshev coefficients and inner-product
+// accumulators of the fused passes, the register-column pass plans
+// (les_col.cu), the case table of the batched ensemble solve
+// (les_ensemble.cu) and the capture of conditional solver loops.
 #pragma once
 
 #include "les_internal.cuh"
