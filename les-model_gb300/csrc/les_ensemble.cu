@@ -112,7 +112,7 @@ __global__ void k_round_begin(BatchCase* cs, int n)
         const int act = !out->done && out->k < C.max_outer && out->iters < C.cap;
         C.act = act;
         if (act) {
-            in->tol = fmax(C.inner_rtol * out->err, out->tol / 3.0);
+            in->tol = fmax(C.inner_rtol * out->err, out->tol / LAST_MARGIN);
             in->max_iter = C.inner_cap;
             in->k = 0;
             in->done = 0;

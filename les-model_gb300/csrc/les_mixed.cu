@@ -131,11 +131,11 @@ __global__ void k_x_add(Geo g, double* __restrict__ x, const float* __restrict__
 }
 
 // Inner state init: tolerance relative to the current outer residual, but no
-// tighter than the outer tolerance needs (a third of it, for the FP32 rounding
-// of the correction): the last correction is not over-solved.
+// tighter than the outer tolerance needs (less the LAST_MARGIN for the FP32
+// rounding of the correction): the last correction is not over-solved.
 __global__ void k_inner_init(SolverState* in, const SolverState* out, double inner_rtol, int max_iter)
 {
-    in->tol = fmax(inner_rtol * out->err, out->tol / 3.0);
+    in->tol = fmax(inner_rtol * out->err, out->tol / LAST_MARGIN);
     in->max_iter = max_iter;
     in->k = 0;
     in->done = 0;

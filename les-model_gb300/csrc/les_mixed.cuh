@@ -98,6 +98,15 @@ __device__ __forceinline__ void acc_prod(Acc& a, float x, float y)
 
 __device__ __forceinline__ double acc_value(const Acc& a) { return (double)a.hi + (double)a.lo; }
 
+// The inner FP32 solve of a correction stops at max(inner_rtol ||r||,
+// tol / LAST_MARGIN): the last correction is not solved further than the
+// outer FP64 test needs, less a margin for the FP32 rounding of the update
+// (the FP64 test still decides, at worst after one more correction).
+// Measured on GB300 (inner iterations per step, 256x128x128 / 512x256x256 /
+// 64-case batch): margin 3: 564 / 986 / 207, 2: 557 / 969 / 202, 1.5: 553 /
+// 962 / 198.
+constexpr double LAST_MARGIN = 1.5;
+
 ChebF cheb_coefs(const les_pcg_opts* o);
 bool fused_supported(const les_pcg_opts* o);
 
