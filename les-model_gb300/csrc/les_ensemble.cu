@@ -542,10 +542,15 @@ les_status les_ensemble_step(les_ensemble* e, const les_step_params* prm, les_st
         for (size_t i = 0; i < n; ++i) e->cs[i]->launches += g->captured[i];
         return LES_OK;
     }
+    // every case's solver state with one synchronisation (pinned mirrors)
+    for (size_t i = 0; i < n && !st; ++i)
+        st = ecuda(e, cudaMemcpyAsync(e->cs[i]->h_state, e->cs[i]->state, 2 * sizeof(SolverState),
+                                      cudaMemcpyDeviceToHost, e->main),
+                   "read states");
+    if (st) return st;
     if ((st = ecuda(e, cudaStreamSynchronize(e->main), "ensemble step"))) return st;
     for (size_t i = 0; i < n; ++i) {
         les_ctx* c = e->cs[i];
-        if ((st = read_state(c))) return efail(e, st, "case " + std::to_string(i) + ": " + c->err);
         const unsigned long long run = graph_step_stats(c, &prm[i], g->captured[i], &stats[i]);
         c->launches += g->batched ? g->captured[i] : run;
     }
