@@ -16,10 +16,10 @@
 //     q = A p, p.q -> alpha
 // Pass B (k_col_b), halo S:
 //     r' = r - alpha q, ||r'||^2
-//     z = M^-1 r': Chebyshev with S = degree-1 stencil levels (the recurrence
-//       of les-model src/pressure.cpp:871-905), temporally blocked along i --
-//       at march step I level k works on plane I-k over the strip grown by
-//       S-k cells; Jacobi (S = 0): z = r' / A_c
+//     z = M^-1 r': Chebyshev with S = degree-1 stencil levels (the polynomial
+//       of les-model src/pressure.cpp:871-905 in three-term form, ColCheb),
+//       temporally blocked along i -- at march step I level k works on plane
+//       I-k over the strip grown by S-k cells; Jacobi (S = 0): z = r' / A_c
 //     r'.z -> beta, rho; convergence on ||r'||
 // The last p and alpha of a solve are left for col_x_update (x += e + alpha p).
 //
@@ -249,7 +249,7 @@ __device__ __forceinline__ void pass_b_finish(const Acc& arr, const Acc& arz, do
 }
 
 template <int S, int TJ, bool FIRST>
-__device__ __forceinline__ void col_b(const Geo& g, const ColMap& m, const Coef& k, const ChebF& cf, float inv_c0,
+__device__ __forceinline__ void col_b(const Geo& g, const ColMap& m, const ColCheb& c3, float inv_c0,
                                       const float* __restrict__ r_in, float* __restrict__ r_out,
                                       const float* __restrict__ q, float* __restrict__ z_out, double* partials,
                                       unsigned* counter, SolverState* st, SolverState* outer, int total_cap, int blk,
@@ -268,7 +268,6 @@ __device__ __forceinline__ void col_b(const Geo& g, const ColMap& m, const Coef&
     if (item < m.items) {
         float rp[S + 1][H];      // r' at planes I - d
         float zr[NL][3][H];      // z_L at planes I - L - d (L = 1 .. S-1 at [L-1])
-        float pcr[NL][2][H];     // pc_L at planes I - L - d
         float vr[H], vq[H];      // r, q of the plane being fetched
         float zS[H];             // the last level's z at its plane, before the stores
 #pragma unroll
@@ -278,10 +277,7 @@ __device__ __forceinline__ void col_b(const Geo& g, const ColMap& m, const Coef&
 #pragma unroll
         for (int L = 0; L < NL; ++L)
 #pragma unroll
-            for (int r = 0; r < H; ++r) {
-                zr[L][0][r] = zr[L][1][r] = zr[L][2][r] = 0.f;
-                pcr[L][0][r] = pcr[L][1][r] = 0.f;
-            }
+            for (int r = 0; r < H; ++r) zr[L][0][r] = zr[L][1][r] = zr[L][2][r] = 0.f;
         auto fetch = [&](int P) {
             if (s.jin) {   // interior row strip: consecutive rows, one validity test
                 const int pl = P < 0 ? -P : P;
@@ -336,43 +332,33 @@ __device__ __forceinline__ void col_b(const Geo& g, const ColMap& m, const Coef&
 #pragma unroll
             for (int LV = 1; LV <= S; ++LV) {
                 const int Pk = I - LV;
-                const float ak = cf.a[LV - 1], bk = cf.b[LV - 1];
-                // plane-uniform coefficients: the outlet plane is an identity
-                // row, the plane before it has no east coefficient; level 1
-                // applies A to z_0 = a0 r', so a0 is folded in
+                // plane-uniform level weights: the outlet plane is an identity
+                // row, the plane before it has no east coefficient
                 const bool ident = Pk == g.nx - 1;
-                const float sc = LV == 1 ? cf.a0 : 1.f;
-                const float cc = sc * (ident ? 1.f : k.c0), cx = ident ? 0.f : sc * k.x1;
-                const float ce = (ident || Pk == g.nx - 2) ? 0.f : sc * k.x1;
-                const float cy = ident ? 0.f : sc * k.y1, cz = ident ? 0.f : sc * k.z1;
+                const float cc = ident ? c3.ci[LV - 1] : c3.cc[LV - 1], cx = ident ? 0.f : c3.cx[LV - 1];
+                const float ce = (ident || Pk == g.nx - 2) ? 0.f : c3.cx[LV - 1];
+                const float cy = ident ? 0.f : c3.cy[LV - 1], cz = ident ? 0.f : c3.cz[LV - 1];
+                const float cr = c3.rr[LV - 1], cg = c3.gg[LV - 1];
                 const bool out_plane = LV == S && Pk >= s.i0 && Pk < s.i1;
                 const int pbase = Pk * g.si + s.j0 * g.sj + s.kl;
                 float s2 = 0.f;
 #pragma unroll
                 for (int r = LV; r < H - LV; ++r) {
-                    float zc, zw, ze, zs, zn, pcp;
-                    if (LV == 1) {   // z_0 = a0 r', pc_0 = r'
+                    float zc, zw, ze, zs, zn;
+                    if (LV == 1) {   // the stencil of z_0 = a0 r' (a0 is in the weights)
                         zc = rp[1][r]; zw = rp[2][r]; ze = rp[0][r];
                         zs = rp[1][r - 1]; zn = rp[1][r + 1];
-                        pcp = rp[1][r];
                     } else {
                         zc = zr[LV - 2][1][r]; zw = zr[LV - 2][2][r]; ze = zr[LV - 2][0][r];
                         zs = zr[LV - 2][1][r - 1]; zn = zr[LV - 2][1][r + 1];
-                        pcp = pcr[LV - 2][1][r];
                     }
                     const float zb = __shfl_up_sync(FULL, zc, 1);
                     const float zt = __shfl_down_sync(FULL, zc, 1);
-                    const float az = cc * zc + cx * zw + ce * ze + cy * (zs + zn) + cz * (zb + zt);
-                    if (LV == 1) zc *= cf.a0;
-                    const float rv = rp[LV][r];
-                    const float pck = fmaf(bk, pcp, rv - az);
-                    const float zk = fmaf(ak, pck, zc);
-                    if (LV < S) {
-                        zr[LV - 1][0][r] = zk;
-                        pcr[LV - 1][0][r] = pck;
-                    } else {
-                        zS[r] = zk;
-                    }
+                    float zk = cc * zc + cx * zw + ce * ze + cy * (zs + zn) + cz * (zb + zt);
+                    if (LV == 2) zk = fmaf(cr, rp[2][r], zk);   // r' and z_0 = a0 r'
+                    if (LV >= 3) zk = fmaf(cr, rp[LV][r], fmaf(cg, zr[LV - 3][2][r], zk));
+                    if (LV < S) zr[LV - 1][0][r] = zk;
+                    else zS[r] = zk;
                 }
                 if (LV == S && out_plane) {   // stores and r'.z of the owned cells
 #pragma unroll
@@ -395,7 +381,6 @@ __device__ __forceinline__ void col_b(const Geo& g, const ColMap& m, const Coef&
                 for (int r = 0; r < H; ++r) {
                     zr[L][2][r] = zr[L][1][r];
                     zr[L][1][r] = zr[L][0][r];
-                    pcr[L][1][r] = pcr[L][0][r];
                 }
         }
     }
@@ -404,13 +389,13 @@ __device__ __forceinline__ void col_b(const Geo& g, const ColMap& m, const Coef&
 }
 
 template <int S, int TJ, bool FIRST>
-__global__ void __launch_bounds__(CT, (TJ == 4 && S <= 3) ? 3 : 2) k_col_b(Geo g, ColMap m, Coef k, ChebF cf, float inv_c0,
+__global__ void __launch_bounds__(CT, (TJ == 4 && S <= 3) ? 3 : 2) k_col_b(Geo g, ColMap m, ColCheb c3, float inv_c0,
                                                const float* __restrict__ r_in, float* __restrict__ r_out,
                                                const float* __restrict__ q, float* __restrict__ z_out,
                                                double* partials, unsigned* counter, SolverState* st,
                                                SolverState* outer, int total_cap)
 {
-    col_b<S, TJ, FIRST>(g, m, k, cf, inv_c0, r_in, r_out, q, z_out, partials, counter, st, outer, total_cap, blockIdx.x,
+    col_b<S, TJ, FIRST>(g, m, c3, inv_c0, r_in, r_out, q, z_out, partials, counter, st, outer, total_cap, blockIdx.x,
                         gridDim.x);
 }
 
@@ -450,7 +435,7 @@ __global__ void __launch_bounds__(CT, (TJ == 4 && S <= 3) ? 3 : 2) k_col_b_batch
     const int c = batch_case(pre, n, blockIdx.x);
     const BatchCase& C = cs[c];
     const int b0 = __ldg(pre + c), nb = __ldg(pre + c + 1) - b0;
-    col_b<S, TJ, FIRST>(C.g, C.mb, Coef{C.c0, C.x1, C.y1, C.z1}, C.cf, C.inv_c0, rin ? C.r1 : C.r0,
+    col_b<S, TJ, FIRST>(C.g, C.mb, C.c3, C.inv_c0, rin ? C.r1 : C.r0,
                         rin ? C.r0 : C.r1, C.q, C.z, C.partials, C.counters + 14, C.in, C.out, C.cap, blockIdx.x - b0,
                         nb);
 }
@@ -471,7 +456,7 @@ __global__ void k_x_update_batch(const BatchCase* __restrict__ cs, const int* __
 // ---- launch plumbing ----------------------------------------------------------
 using KA = void (*)(Geo, ColMap, Coef, const float*, const float*, float*, float*, float*, double*, unsigned*,
                     SolverState*, int);
-using KB = void (*)(Geo, ColMap, Coef, ChebF, float, const float*, float*, const float*, float*, double*, unsigned*,
+using KB = void (*)(Geo, ColMap, ColCheb, float, const float*, float*, const float*, float*, double*, unsigned*,
                     SolverState*, SolverState*, int);
 
 KA pick_a(int tj, bool first)
@@ -540,6 +525,36 @@ ColMap col_map(les_ctx* c, const void* fn, int halo, int tj, int ci_force)
 
 namespace les {
 
+ColCheb col_cheb(const les_pcg_opts* o, float c0f, float x1f, float y1f, float z1f)
+{
+    ColCheb t{};
+    const int S = o->precond == LES_PC_CHEBYSHEV ? o->degree - 1 : 0;
+    if (S <= 0) return t;
+    // a_k, b_k as the reference's recurrence forms them (src/pressure.cpp:878-899)
+    const double d = (o->lambda_max + o->lambda_min) / 2.0, cw = (o->lambda_max - o->lambda_min) / 2.0;
+    const double c0 = c0f, x1 = x1f, y1 = y1f, z1 = z1f, a0 = 2.0 / d;
+    double ap = a0;   // a_{k-1}
+    for (int k = 1; k <= S && k <= 6; ++k) {
+        const double b = (cw * ap / 2.0) * (cw * ap / 2.0);
+        const double a = 1.0 / (d - b);
+        const double gk = a * b / ap;
+        const double sc = k == 1 ? a0 : 1.0;   // level 1 applies its stencil to r'
+        double cc = sc * (1.0 + gk) - a * sc * c0, ci = sc * (1.0 + gk) - a * sc;
+        double rr = a, gg = -gk;
+        if (k == 1) { cc += a; ci += a; rr = 0.0; gg = 0.0; }   // r' is the centre value
+        if (k == 2) { rr = a - gk * a0; gg = 0.0; }            // z_0 = a0 r' at the centre
+        t.cc[k - 1] = (float)cc;
+        t.ci[k - 1] = (float)ci;
+        t.cx[k - 1] = (float)(-a * sc * x1);
+        t.cy[k - 1] = (float)(-a * sc * y1);
+        t.cz[k - 1] = (float)(-a * sc * z1);
+        t.rr[k - 1] = (float)rr;
+        t.gg[k - 1] = (float)gg;
+        ap = a;
+    }
+    return t;
+}
+
 bool col_supported(const les_ctx* c, const les_pcg_opts* o)
 {
     if (!(c->fused == 1 && !c->opt_tma && c->stencil_mode == 1 && c->code_plain && fused_supported(o))) return false;
@@ -552,7 +567,7 @@ bool col_supported(const les_ctx* c, const les_pcg_opts* o)
 les_status col_plan(les_ctx* c, const les_pcg_opts* o, ViewF A, SolverState* in, SolverState* out, ColPlan& P)
 {
     P.S = o->precond == LES_PC_JACOBI ? 0 : o->degree - 1;
-    P.cf = cheb_coefs(o);
+    P.c3 = col_cheb(o, A.k.c0, A.k.x1, A.k.y1, A.k.z1);
     P.inv_c0 = 1.f / A.k.c0;
     P.A = A;
     P.in = in;
@@ -583,7 +598,7 @@ les_status col_pass_b(les_ctx* c, const ColPlan& P, bool first, int rin)
 {
     float* r[2] = {c->f[0], c->f[6]};
     float *z = c->f[1], *q = c->f[4];
-    launch_pdl(c, PROF_IN_CHEB, pick_b(P.S, P.mb.tj, first), P.blocks_b, CT, c->g, P.mb, coef_of(P), P.cf, P.inv_c0,
+    launch_pdl(c, PROF_IN_CHEB, pick_b(P.S, P.mb.tj, first), P.blocks_b, CT, c->g, P.mb, P.c3, P.inv_c0,
              (const float*)r[rin], r[rin ^ 1], (const float*)q, z, c->partials, c->counters + 14, P.in, P.out, P.cap);
     return check_launch(c, "column pass B");
 }

@@ -230,7 +230,7 @@ les_status batch_plan(les_ensemble* e, const les_step_params* prm, les_ensemble:
         C.x1 = A32.k.x1;
         C.y1 = A32.k.y1;
         C.z1 = A32.k.z1;
-        C.cf = cheb_coefs(&o);
+        C.c3 = col_cheb(&o, A32.k.c0, A32.k.x1, A32.k.y1, A32.k.z1);
         C.inv_c0 = 1.f / A32.k.c0;
         C.r0 = c->f[0]; C.r1 = c->f[6]; C.z = c->f[1]; C.p0 = c->f[2]; C.p1 = c->f[3]; C.q = c->f[4]; C.e = c->f[5];
         C.x = c->slot[LES_P];

@@ -72,6 +72,20 @@ struct ChebF {
     float a[8], b[8];
 };
 
+// The same polynomial in three-term form, as the column passes apply it.
+// With pc_{k-1} = (z_{k-1} - z_{k-2}) / a_{k-1} (z_{-1} = 0, so pc_0 = r),
+// level k is  z_k = (1 + g_k) z_{k-1} - g_k z_{k-2} + a_k (r - A z_{k-1}),
+// g_k = a_k b_k / a_{k-1}.  A's plane-uniform coefficients are folded into
+// per-level weights, so a level is one 7-point stencil plus the r and z_{k-2}
+// terms.  Level 1 reads r' directly (z_0 = a0 r', its r term joins the
+// centre weight); level 2's z_{k-2} = z_0 term joins its r term.
+struct ColCheb {
+    float cc[6], ci[6];          // centre weight; on the outlet plane's identity rows
+    float cx[6], cy[6], cz[6];   // neighbour weights along i, j, k
+    float rr[6], gg[6];          // weights of r' and of z_{k-2} at the centre
+};
+ColCheb col_cheb(const les_pcg_opts* o, float c0, float x1, float y1, float z1);
+
 // Inner products of the fused passes: per-thread double-float (TwoSum /
 // TwoProd, ~48-bit significand) accumulation, summed across threads and
 // blocks in FP64.  GB300's FP64 pipe is ~70x slower than its FP32 pipe.
@@ -123,7 +137,7 @@ struct ColMap {
 
 struct ColPlan {
     int S = 0;             // Chebyshev levels (degree - 1); 0 = Jacobi
-    ChebF cf{};
+    ColCheb c3{};
     float inv_c0 = 1.f;
     ColMap ma{}, mb{};
     int blocks_a = 0, blocks_b = 0;
@@ -153,7 +167,7 @@ struct BatchCase {
     Geo g;
     ColMap ma, mb;                 // column-pass work splits
     float c0, x1, y1, z1;          // plane-uniform FP32 coefficients
-    ChebF cf;
+    ColCheb c3;                    // pass B's Chebyshev level weights
     float inv_c0;
     float *r0, *r1, *z, *p0, *p1, *q, *e;   // FP32 inner vectors
     double* x;                     // FP64 solution (the pressure slot)
