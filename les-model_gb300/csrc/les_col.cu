@@ -41,6 +41,7 @@
 // recomputed by every strip that needs them (values of lanes and rows past
 // the shrinking halo are never used).
 #include <cmath>
+#include <type_traits>
 
 #include "les_internal.cuh"
 #include "les_mixed.cuh"
@@ -62,8 +63,43 @@ struct StripPos {
     int i0, i1;    // owned planes [i0, i1)
     int kl;        // this lane's k after reflection at the walls (-1: not loaded)
     unsigned own;  // bit r: cell of row r owned by this lane
-    bool jin;      // every row of the strip inside the grid: rows need no reflection
+    int rows;      // row pattern (RowsMode) of the strip
 };
+
+// How the rows of a strip map onto grid rows.  Row r of a strip lies at
+// j = j0 + r, reflected into [0, ny) about the wall rows.  The interior
+// strips need no reflection; the first strip (j0 = -HALO) reflects about its
+// row HALO and, when ny is a multiple of the strip's owned rows, the last
+// strip about its row H - HALO - 1: both patterns are known at compile time,
+// so these strips fetch as cheaply as the interior ones.  Any other strip
+// (a grid only a few strips wide, a ragged last strip) reflects per row.
+enum RowsMode { ROWS_PLAIN = 0, ROWS_FIRST = 1, ROWS_LAST = 2, ROWS_ANY = 3 };
+
+// reflected grid row of strip row r, minus j0
+template <int MODE, int HALO, int H>
+__device__ __forceinline__ int row_rel(int r, int j0, int ny)
+{
+    if (MODE == ROWS_PLAIN) return r;
+    if (MODE == ROWS_FIRST) return (r < HALO ? HALO - r : r - HALO) + HALO;
+    if (MODE == ROWS_LAST) {
+        constexpr int e = H - HALO - 1;
+        return r <= e ? r : 2 * e - r;
+    }
+    int j = j0 + r;
+    j = j < 0 ? -j : j;
+    j = min(j, 2 * (ny - 1) - j);
+    return max(j, 0) - j0;   // rows beyond one reflection are never used: any row in the grid
+}
+
+// calls f(integral_constant<int, mode>) for the strip's row pattern
+template <class F>
+__device__ __forceinline__ void with_rows(int mode, F&& f)
+{
+    if (mode == ROWS_PLAIN) f(std::integral_constant<int, ROWS_PLAIN>{});
+    else if (mode == ROWS_FIRST) f(std::integral_constant<int, ROWS_FIRST>{});
+    else if (mode == ROWS_LAST) f(std::integral_constant<int, ROWS_LAST>{});
+    else f(std::integral_constant<int, ROWS_ANY>{});
+}
 
 // reflection of index x into [0, n) about the end cells (-1 if still outside)
 __device__ __forceinline__ int reflect(int x, int n)
@@ -81,7 +117,11 @@ __device__ __forceinline__ StripPos strip_pos(const Geo& g, const ColMap& m, int
     const int jt = rest % m.tiles_j, ch = rest / m.tiles_j;
     const int kg = kt * m.tk - HALO + lane;
     s.j0 = jt * TJ - HALO;
-    s.jin = s.j0 >= 0 && s.j0 + TJ + 2 * HALO <= g.ny;
+    constexpr int H = TJ + 2 * HALO;
+    if (s.j0 >= 0 && s.j0 + H <= g.ny) s.rows = ROWS_PLAIN;
+    else if (s.j0 == -HALO && H - HALO <= g.ny) s.rows = ROWS_FIRST;
+    else if (s.j0 >= 0 && s.j0 + H == g.ny + HALO) s.rows = ROWS_LAST;
+    else s.rows = ROWS_ANY;
     s.i0 = ch * m.ci;
     s.i1 = min(g.nx, s.i0 + m.ci);
     s.kl = reflect(kg, g.nz);
@@ -91,15 +131,6 @@ __device__ __forceinline__ StripPos strip_pos(const Geo& g, const ColMap& m, int
     for (int r = HALO; r < HALO + TJ; ++r)
         if (kown && s.j0 + r < g.ny) s.own |= 1u << r;
     return s;
-}
-
-// offset of row r of plane P in the reflected field, or -1 (not loaded:
-// planes past the outlet are never read)
-__device__ __forceinline__ int row_off(const Geo& g, const StripPos& s, int P, int r)
-{
-    const int jl = reflect(s.j0 + r, g.ny);
-    const int pl = P < 0 ? -P : P;
-    return (jl >= 0 && s.kl >= 0 && pl < g.nx) ? pl * g.si + jl * g.sj + s.kl : -1;
 }
 
 // ---- pass A -----------------------------------------------------------------
@@ -128,10 +159,11 @@ __device__ __forceinline__ void col_a(const Geo& g, const ColMap& m, const Coef&
         for (int r = 0; r < H; ++r) p0[r] = p1[r] = p2[r] = 0.f;
         auto fetch = [&](int P) {
             const bool pown = P >= s.i0 && P < s.i1;
-            if (s.jin) {   // interior row strip: consecutive rows, one validity test
-                const int pl = P < 0 ? -P : P;
-                const bool ok = s.kl >= 0 && pl < g.nx;
-                int id = pl * g.si + s.j0 * g.sj + s.kl;
+            const int pl = P < 0 ? -P : P;   // plane -m reads plane m; planes past the outlet are not read
+            const bool ok = s.kl >= 0 && pl < g.nx;
+            const int base = pl * g.si + s.j0 * g.sj + s.kl;
+            if (s.rows == ROWS_PLAIN) {
+                int id = base;
 #pragma unroll
                 for (int r = 0; r < H; ++r, id += g.sj) {
                     vz[r] = ok ? z[id] : 0.f;
@@ -140,13 +172,16 @@ __device__ __forceinline__ void col_a(const Geo& g, const ColMap& m, const Coef&
                 }
                 return;
             }
+            with_rows(s.rows, [&](auto md) {
+                constexpr int MD = decltype(md)::value;
 #pragma unroll
-            for (int r = 0; r < H; ++r) {
-                const int id = row_off(g, s, P, r);
-                vz[r] = id >= 0 ? z[id] : 0.f;
-                vp[r] = (!FIRST && id >= 0) ? pold[id] : 0.f;
-                if (r >= 1 && r <= TJ) ve[r - 1] = (!FIRST && pown && ((s.own >> r) & 1u)) ? e[id] : 0.f;
-            }
+                for (int r = 0; r < H; ++r) {
+                    const int id = base + row_rel<MD, 1, H>(r, s.j0, g.ny) * g.sj;
+                    vz[r] = ok ? z[id] : 0.f;
+                    vp[r] = (!FIRST && ok) ? pold[id] : 0.f;
+                    if (r >= 1 && r <= TJ) ve[r - 1] = (!FIRST && pown && ((s.own >> r) & 1u)) ? e[id] : 0.f;
+                }
+            });
         };
         fetch(s.i0 - 1);
         for (int P = s.i0 - 1; P <= s.i1; ++P) {
@@ -279,23 +314,18 @@ __device__ __forceinline__ void col_b(const Geo& g, const ColMap& m, const ColCh
 #pragma unroll
             for (int r = 0; r < H; ++r) zr[L][0][r] = zr[L][1][r] = zr[L][2][r] = 0.f;
         auto fetch = [&](int P) {
-            if (s.jin) {   // interior row strip: consecutive rows, one validity test
-                const int pl = P < 0 ? -P : P;
-                const bool ok = s.kl >= 0 && pl < g.nx;
-                int id = pl * g.si + s.j0 * g.sj + s.kl;
+            const int pl = P < 0 ? -P : P;   // plane -m reads plane m; planes past the outlet are not read
+            const bool ok = s.kl >= 0 && pl < g.nx;
+            const int base = pl * g.si + s.j0 * g.sj + s.kl;
+            with_rows(s.rows, [&](auto md) {
+                constexpr int MD = decltype(md)::value;
 #pragma unroll
-                for (int r = 0; r < H; ++r, id += g.sj) {
+                for (int r = 0; r < H; ++r) {
+                    const int id = base + row_rel<MD, S, H>(r, s.j0, g.ny) * g.sj;
                     vr[r] = ok ? r_in[id] : 0.f;
                     vq[r] = (!FIRST && ok) ? q[id] : 0.f;
                 }
-                return;
-            }
-#pragma unroll
-            for (int r = 0; r < H; ++r) {
-                const int id = row_off(g, s, P, r);
-                vr[r] = id >= 0 ? r_in[id] : 0.f;
-                vq[r] = (!FIRST && id >= 0) ? q[id] : 0.f;
-            }
+            });
         };
         fetch(s.i0 - S);
         for (int I = s.i0 - S; I < s.i1 + S; ++I) {
