@@ -61,9 +61,11 @@ struct Coef {
 struct StripPos {
     int j0;        // j of row 0
     int i0, i1;    // owned planes [i0, i1)
-    int kl;        // this lane's k after reflection at the walls (-1: not loaded)
+    int kl;        // this lane's k after reflection at the walls
     unsigned own;  // bit r: cell of row r owned by this lane
     int rows;      // row pattern (RowsMode) of the strip
+    bool kown;     // this lane's k is owned
+    bool allrows;  // every owned row of the strip is inside the grid: ownership is kown
 };
 
 // How the rows of a strip map onto grid rows.  Row r of a strip lies at
@@ -124,8 +126,11 @@ __device__ __forceinline__ StripPos strip_pos(const Geo& g, const ColMap& m, int
     else s.rows = ROWS_ANY;
     s.i0 = ch * m.ci;
     s.i1 = min(g.nx, s.i0 + m.ci);
-    s.kl = reflect(kg, g.nz);
+    // lanes past one reflection are never used; they read any cell of the grid
+    s.kl = max(reflect(kg, g.nz), 0);
     const bool kown = kg >= 0 && kg < g.nz && lane >= HALO && lane < HALO + m.tk;
+    s.kown = kown;
+    s.allrows = s.j0 + HALO + TJ <= g.ny;
     s.own = 0u;
 #pragma unroll
     for (int r = HALO; r < HALO + TJ; ++r)
@@ -159,16 +164,22 @@ __device__ __forceinline__ void col_a(const Geo& g, const ColMap& m, const Coef&
         for (int r = 0; r < H; ++r) p0[r] = p1[r] = p2[r] = 0.f;
         auto fetch = [&](int P) {
             const bool pown = P >= s.i0 && P < s.i1;
-            const int pl = P < 0 ? -P : P;   // plane -m reads plane m; planes past the outlet are not read
-            const bool ok = s.kl >= 0 && pl < g.nx;
+            const int pl = P < 0 ? -P : P;   // plane -m reads plane m
+            if (pl >= g.nx) {                // planes past the outlet are not read
+#pragma unroll
+                for (int r = 0; r < H; ++r) vz[r] = vp[r] = 0.f;
+                return;
+            }
+            // e only on owned planes (its values on cells this lane does not
+            // own are never used)
             const int base = pl * g.si + s.j0 * g.sj + s.kl;
             if (s.rows == ROWS_PLAIN) {
                 int id = base;
 #pragma unroll
                 for (int r = 0; r < H; ++r, id += g.sj) {
-                    vz[r] = ok ? z[id] : 0.f;
-                    vp[r] = (!FIRST && ok) ? pold[id] : 0.f;
-                    if (r >= 1 && r <= TJ) ve[r - 1] = (!FIRST && pown && ((s.own >> r) & 1u)) ? e[id] : 0.f;
+                    vz[r] = z[id];
+                    vp[r] = FIRST ? 0.f : pold[id];
+                    if (r >= 1 && r <= TJ) ve[r - 1] = (!FIRST && pown) ? e[id] : 0.f;
                 }
                 return;
             }
@@ -177,9 +188,9 @@ __device__ __forceinline__ void col_a(const Geo& g, const ColMap& m, const Coef&
 #pragma unroll
                 for (int r = 0; r < H; ++r) {
                     const int id = base + row_rel<MD, 1, H>(r, s.j0, g.ny) * g.sj;
-                    vz[r] = ok ? z[id] : 0.f;
-                    vp[r] = (!FIRST && ok) ? pold[id] : 0.f;
-                    if (r >= 1 && r <= TJ) ve[r - 1] = (!FIRST && pown && ((s.own >> r) & 1u)) ? e[id] : 0.f;
+                    vz[r] = z[id];
+                    vp[r] = FIRST ? 0.f : pold[id];
+                    if (r >= 1 && r <= TJ) ve[r - 1] = (!FIRST && pown) ? e[id] : 0.f;
                 }
             });
         };
@@ -189,14 +200,19 @@ __device__ __forceinline__ void col_a(const Geo& g, const ColMap& m, const Coef&
             for (int r = 0; r < H; ++r) p0[r] = FIRST ? vz[r] : fmaf(beta, vp[r], vz[r]);
             if (P >= s.i0 && P < s.i1) {
                 const int base = P * g.si + s.j0 * g.sj + s.kl;   // owned cells: no reflection
+                auto outp = [&](auto all) {
+                    constexpr bool AL = decltype(all)::value;
 #pragma unroll
-                for (int r = 1; r <= TJ; ++r) {
-                    if ((s.own >> r) & 1u) {
-                        const int id = base + r * g.sj;
-                        pnew[id] = p0[r];
-                        e[id] = FIRST ? 0.f : fmaf(aprev, vp[r], ve[r - 1]);
+                    for (int r = 1; r <= TJ; ++r) {
+                        if (AL ? s.kown : ((s.own >> r) & 1u)) {
+                            const int id = base + r * g.sj;
+                            pnew[id] = p0[r];
+                            e[id] = FIRST ? 0.f : fmaf(aprev, vp[r], ve[r - 1]);
+                        }
                     }
-                }
+                };
+                if (s.allrows) outp(std::true_type{});
+                else outp(std::false_type{});
             }
             if (P < s.i1) fetch(P + 1);
             // q = A p at plane C = P - 1
@@ -218,12 +234,18 @@ __device__ __forceinline__ void col_a(const Geo& g, const ColMap& m, const Coef&
                     const float pt = __shfl_down_sync(FULL, pc, 1);
                     qv[r] = cc * pc + cx * p2[r] + ce * p0[r] + cy * (p1[r - 1] + p1[r + 1]) + cz * (pb + pt);
                 }
+                auto outq = [&](auto all) {
+                    constexpr bool AL = decltype(all)::value;
 #pragma unroll
-                for (int r = 1; r <= TJ; ++r) {
-                    const bool o = (s.own >> r) & 1u;
-                    if (o) q[cb + r * g.sj] = qv[r];
-                    sq = fmaf(o ? p1[r] : 0.f, qv[r], sq);
-                }
+                    for (int r = 1; r <= TJ; ++r) {
+                        const bool o = AL ? s.kown : ((s.own >> r) & 1u);
+                        if (o) q[cb + r * g.sj] = qv[r];
+                        sq = fmaf(AL || o ? p1[r] : 0.f, qv[r], sq);
+                    }
+                    if (AL && !s.kown) sq = 0.f;
+                };
+                if (s.allrows) outq(std::true_type{});
+                else outq(std::false_type{});
                 acc_add(acc, sq);
             }
 #pragma unroll
@@ -314,8 +336,10 @@ __device__ __forceinline__ void col_b(const Geo& g, const ColMap& m, const ColCh
 #pragma unroll
             for (int r = 0; r < H; ++r) zr[L][0][r] = zr[L][1][r] = zr[L][2][r] = 0.f;
         auto fetch = [&](int P) {
-            const int pl = P < 0 ? -P : P;   // plane -m reads plane m; planes past the outlet are not read
-            const bool ok = s.kl >= 0 && pl < g.nx;
+            // plane -m reads plane m; planes past the outlet are not read (a
+            // select, not a branch: the loads stay in the plane's basic block)
+            const int pl = P < 0 ? -P : P;
+            const bool ok = pl < g.nx;
             const int base = pl * g.si + s.j0 * g.sj + s.kl;
             with_rows(s.rows, [&](auto md) {
                 constexpr int MD = decltype(md)::value;
@@ -342,20 +366,28 @@ __device__ __forceinline__ void col_b(const Geo& g, const ColMap& m, const ColCh
                 // the stores and sums of the owned cells
 #pragma unroll
                 for (int r = 0; r < H; ++r) rp[0][r] = FIRST ? vr[r] : fmaf(-alpha, vq[r], vr[r]);
-                if (pown) {
+                // owned cells: every row of the strip or the rows inside the
+                // grid (sums over all rows, then the lane's share)
+                auto out0 = [&](auto all) {
+                    constexpr bool AL = decltype(all)::value;
 #pragma unroll
                     for (int r = S; r < S + TJ; ++r) {
                         const float rv = rp[0][r];
-                        const bool o = (s.own >> r) & 1u;
+                        const bool o = AL ? s.kown : ((s.own >> r) & 1u);
                         const int id = base + r * g.sj;
                         if (o) r_out[id] = rv;
-                        srr = fmaf(o ? rv : 0.f, rv, srr);
+                        srr = fmaf(AL || o ? rv : 0.f, rv, srr);
                         if (S == 0) {
                             const float zv = rv * dinv;
                             if (o) z_out[id] = zv;
-                            srz = fmaf(o ? rv : 0.f, zv, srz);
+                            srz = fmaf(AL || o ? rv : 0.f, zv, srz);
                         }
                     }
+                    if (AL && !s.kown) srr = srz = 0.f;
+                };
+                if (pown) {
+                    if (s.allrows) out0(std::true_type{});
+                    else out0(std::false_type{});
                     acc_add(arr, srr);
                     if (S == 0) acc_add(arz, srz);
                 }
@@ -394,12 +426,18 @@ __device__ __forceinline__ void col_b(const Geo& g, const ColMap& m, const ColCh
                     else zS[r] = zk;
                 }
                 if (LV == S && out_plane) {   // stores and r'.z of the owned cells
+                    auto outS = [&](auto all) {
+                        constexpr bool AL = decltype(all)::value;
 #pragma unroll
-                    for (int r = S; r < S + TJ; ++r) {
-                        const bool o = (s.own >> r) & 1u;
-                        if (o) z_out[pbase + r * g.sj] = zS[r];
-                        s2 = fmaf(o ? rp[S][r] : 0.f, zS[r], s2);
-                    }
+                        for (int r = S; r < S + TJ; ++r) {
+                            const bool o = AL ? s.kown : ((s.own >> r) & 1u);
+                            if (o) z_out[pbase + r * g.sj] = zS[r];
+                            s2 = fmaf(AL || o ? rp[S][r] : 0.f, zS[r], s2);
+                        }
+                        if (AL && !s.kown) s2 = 0.f;
+                    };
+                    if (s.allrows) outS(std::true_type{});
+                    else outS(std::false_type{});
                     acc_add(arz, s2);
                 }
             }
