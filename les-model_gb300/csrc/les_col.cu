@@ -353,8 +353,10 @@ __device__ __forceinline__ void col_b(const Geo& g, const ColMap& m, const ColCh
         };
         fetch(s.i0 - S);
         // three steps per loop pass: the three-plane z rings rotate by
-        // register renaming instead of moves
-#pragma unroll 3
+        // register renaming instead of moves (up to 4 levels; deeper ones
+        // would spill)
+        constexpr int UNROLL = S <= 4 ? 3 : 1;
+#pragma unroll UNROLL
         for (int I = s.i0 - S; I < s.i1 + S; ++I) {
             // ---- level 0 at plane I
             {
