@@ -138,24 +138,238 @@ __device__ __forceinline__ StripPos strip_pos(const Geo& g, const ColMap& m, int
     return s;
 }
 
+// ---- the grid sums between the passes ------------------------------------------
+// Two protocols.  Last block (DEFER = false, the batched ensemble kernels):
+// every block leaves its partial sums, and the block that arrives last
+// (fence + atomic counter) adds them up and updates the solver state before
+// the kernel ends.  Deferred (DEFER = true, the single-case kernels): a pass
+// only leaves its block partials; every block of the NEXT pass adds them up
+// itself, in the same fixed order, right after its dependency wait, and its
+// block 0 writes the state.  The deferred form takes the fence, the atomic
+// and the serial final sum off the end of every pass (3.8 us of pass A's and
+// 6.6 us of pass B's 57 us iteration at 256x128x128), at the price of a
+// parallel sum at the start of the next one.  The decisions stay those of
+// the last-block form: pass A of iteration k+1 makes the convergence test on
+// ||r_k||, forms beta and rho from pass B's partials and, if the solve ends,
+// stores the final state; pass B forms alpha from pass A's partials and
+// commits the iteration count and rho.  A block only writes state fields
+// that no block of its own kernel reads (rho_next is the rho handed from
+// pass A to pass B), so the kernels need no ordering among their blocks.
+// Which hand-offs of the single-case kernels are deferred: pass A -> pass B
+// (alpha) and pass B -> pass A (beta, the convergence test).
+#ifndef COL_DEFER_AB
+#define COL_DEFER_AB 1
+#endif
+#ifndef COL_DEFER_BA
+#define COL_DEFER_BA 1
+#endif
+
+struct Defer {
+    const float2* pin;   // the previous pass's block partials, (hi, lo) pairs
+    int nb_in;           // blocks of the previous pass
+    float2* pout;        // this pass's block partials
+};
+
+// Double-float sums on the FP32 pipe (GB300 runs FP64 arithmetic at a small
+// fraction of its FP32 rate, and FP64 block sums in every block of a pass
+// cost microseconds): the sum of two (hi, lo) pairs by TwoSum of the high
+// parts, renormalised; about 48 significant bits, as the per-thread
+// accumulators keep.
+__device__ __forceinline__ Acc df_add(const Acc& a, const Acc& b)
+{
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bp = __fsub_rn(s, a.hi);
+    const float err = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bp)), __fsub_rn(b.hi, bp));
+    const float lo = __fadd_rn(__fadd_rn(a.lo, b.lo), err);
+    Acc r;
+    r.hi = __fadd_rn(s, lo);
+    r.lo = __fsub_rn(lo, __fsub_rn(r.hi, s));
+    return r;
+}
+
+// Block sum of NV pairs in a fixed order; the totals in thread 0.
+// sm: NV * 32 float2.
+template <int NV>
+__device__ __forceinline__ void block_sum_df(Acc (&v)[NV], float2* sm)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            Acc t;
+            t.hi = __shfl_down_sync(0xffffffffu, v[q].hi, o);
+            t.lo = __shfl_down_sync(0xffffffffu, v[q].lo, o);
+            v[q] = df_add(v[q], t);
+        }
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) sm[q * 32 + warp] = make_float2(v[q].hi, v[q].lo);
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            const float2 t = lane < nw ? sm[q * 32 + lane] : make_float2(0.f, 0.f);
+            v[q].hi = t.x;
+            v[q].lo = t.y;
+        }
+#pragma unroll
+        for (int q = 0; q < NV; ++q)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                Acc t;
+                t.hi = __shfl_down_sync(0xffffffffu, v[q].hi, o);
+                t.lo = __shfl_down_sync(0xffffffffu, v[q].lo, o);
+                v[q] = df_add(v[q], t);
+            }
+    }
+}
+
+// A pass's block partials: block_sum_df, then (hi, lo) at [q * nb + blk].
+template <int NV>
+__device__ __forceinline__ void put_partials(Acc (&v)[NV], float2* sm, float2* pout, int blk, int nb)
+{
+    block_sum_df<NV>(v, sm);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) pout[q * nb + blk] = make_float2(v[q].hi, v[q].lo);
+}
+
+// Sums NV vectors of nb block partials (thread-strided, then the block
+// tree: a fixed order); the totals as doubles in thread 0.
+template <int NV>
+__device__ __forceinline__ void sum_partials(const float2* __restrict__ part, int nb, double (&v)[NV], float2* sm)
+{
+    Acc acc[NV];
+    for (int b = threadIdx.x; b < nb; b += blockDim.x)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            const float2 t = __ldcg(part + q * nb + b);
+            Acc x;
+            x.hi = t.x;
+            x.lo = t.y;
+            acc[q] = df_add(acc[q], x);
+        }
+    block_sum_df<NV>(acc, sm);
+#pragma unroll
+    for (int q = 0; q < NV; ++q) v[q] = (double)acc[q].hi + (double)acc[q].lo;
+}
+
+// The deferred heads of the two passes, kept out of line: inlined, their
+// FP64 scalars and barriers changed how the march around them was compiled
+// (pass A's march ran 20 % slower).  Both return `end` (leave the kernel:
+// the solve is done) in every thread of the block.
+struct HeadOut {
+    int end;
+    float coef;   // pass A: beta; pass B: alpha
+};
+
+// Pass A: pass B's sums ||r'||^2, r'.z; the convergence test and the state
+// in thread 0 (FP64), block 0 writing.
+template <bool FIRST>
+__device__ __noinline__ HeadOut head_a(const float2* __restrict__ pin, int nb_in, SolverState* st,
+                                       SolverState* outer, int total_cap, int pslot, int blk)
+{
+    __shared__ double sm[64];
+    __shared__ HeadOut so;
+    double v[2];
+    if (threadIdx.x == 0) so.end = st->done;
+    __syncthreads();
+    if (so.end) return so;
+    __syncthreads();
+    sum_partials<2>(pin, nb_in, v, reinterpret_cast<float2*>(sm));
+    if (threadIdx.x == 0) {
+        const bool w0 = blk == 0;
+        int status = -1;
+        if (FIRST) {
+            if (w0) st->rho_next = v[1];
+            so.coef = 0.f;
+        } else {
+            const double err = sqrt(v[0]), rho_old = st->rho;
+            const int kk = st->k, total = outer->iters;   // committed by pass B
+            if (err < st->tol) status = LES_OK;
+            else if (!isfinite(err)) status = LES_NONFINITE;
+            else if (kk >= st->max_iter || total >= total_cap) status = LES_NOT_CONVERGED;
+            const double b = v[1] / rho_old;
+            so.coef = (float)b;
+            if (w0) {
+                st->err = err;
+                st->beta = b;
+                if (status >= 0) {   // the solve ends at iteration kk: the final state
+                    st->rho = v[1];
+                    st->status = status;
+                    st->done = 1;
+                } else {
+                    st->rho_next = v[1];
+                }
+            }
+        }
+        if (w0 && status < 0) st->buf = pslot;   // buffer holding this iteration's p
+        so.end = status >= 0;                    // no work after the last iteration
+    }
+    __syncthreads();
+    return so;
+}
+
+// Pass B: pass A's sum p.q -> alpha (thread 0, FP64); with pass B's own sums
+// deferred too, pass A hands rho over in rho_next and this pass commits the
+// iteration, otherwise rho is current and this pass's last block does the
+// state at its end.
+template <bool BOUT>
+__device__ __noinline__ HeadOut head_b(const float2* __restrict__ pin, int nb_in, SolverState* st,
+                                       SolverState* outer, int blk)
+{
+    __shared__ double sm[64];
+    __shared__ HeadOut so;
+    double v[1];
+    if (threadIdx.x == 0) so.end = st->done;
+    __syncthreads();
+    if (so.end) return so;
+    __syncthreads();
+    sum_partials<1>(pin, nb_in, v, reinterpret_cast<float2*>(sm));
+    if (threadIdx.x == 0) {
+        const double rho = BOUT ? st->rho_next : st->rho, a = rho / v[0];
+        so.coef = (float)a;
+        if (blk == 0) {
+            st->alpha = a;
+            if (BOUT) {
+                st->rho = rho;
+                st->k = st->k + 1;
+                outer->iters = outer->iters + 1;
+            }
+        }
+    }
+    __syncthreads();
+    return so;
+}
+
 // ---- pass A -----------------------------------------------------------------
 // blk / nblk: this block among the blocks of the pass (one case's blocks in
 // a batched launch)
-template <int TJ, bool FIRST>
+template <int TJ, bool FIRST, bool AIN, bool AOUT>
 __device__ __forceinline__ void col_a(const Geo& g, const ColMap& m, const Coef& k, const float* __restrict__ z,
                                       const float* __restrict__ pold, float* __restrict__ pnew, float* __restrict__ q,
                                       float* __restrict__ e, double* partials, unsigned* counter, SolverState* st,
-                                      int pslot, int blk, int nblk)
+                                      int pslot, int blk, int nblk, const Defer& df, SolverState* outer, int total_cap)
 {
     constexpr int H = TJ + 2;
-    __shared__ double sm[32];
+    __shared__ double sm[64];
     const int lane = threadIdx.x & 31;
     const int item = blk * CWPB + (threadIdx.x >> 5);
     const StripPos s = strip_pos<1, TJ>(g, m, item, lane);   // from the arguments only
     dep_wait();
-    if (st->done) return;
-    const float beta = FIRST ? 0.f : (float)st->beta;
+    float beta = 0.f;
+    if (AIN) {   // pass B's sums, the decision and the state
+        const HeadOut h = head_a<FIRST>(df.pin, df.nb_in, st, outer, total_cap, pslot, blk);
+        if (h.end) return;
+        beta = h.coef;
+    } else {
+        if (st->done) return;
+        if (!FIRST) beta = (float)st->beta;
+    }
     const float aprev = FIRST ? 0.f : (float)st->alpha;
+    if (!AIN && AOUT && blk == 0 && threadIdx.x == 0) st->buf = pslot;   // buffer holding this iteration's p
     Acc acc;
     if (item < m.items) {
         float p0[H], p1[H], p2[H];   // p at planes P, P-1, P-2
@@ -256,6 +470,11 @@ __device__ __forceinline__ void col_a(const Geo& g, const ColMap& m, const Coef&
         }
     }
     dep_signal();
+    if (AOUT) {
+        Acc v[1] = {acc};
+        put_partials<1>(v, reinterpret_cast<float2*>(sm), df.pout, blk, nblk);
+        return;
+    }
     double v[1] = {acc_value(acc)};
     if (last_block_sum<1>(v, partials, counter, sm, blk, nblk)) {
         if (threadIdx.x == 0) {
@@ -270,9 +489,10 @@ __global__ void __launch_bounds__(CT, TJ == 8 ? 4 : 2) k_col_a(Geo g, ColMap m, 
                                                              const float* __restrict__ pold, float* __restrict__ pnew,
                                                              float* __restrict__ q, float* __restrict__ e,
                                                              double* partials, unsigned* counter, SolverState* st,
-                                                             int pslot)
+                                                             int pslot, Defer df, SolverState* outer, int total_cap)
 {
-    col_a<TJ, FIRST>(g, m, k, z, pold, pnew, q, e, partials, counter, st, pslot, blockIdx.x, gridDim.x);
+    col_a<TJ, FIRST, COL_DEFER_BA, COL_DEFER_AB>(g, m, k, z, pold, pnew, q, e, partials, counter, st, pslot,
+                                                  blockIdx.x, gridDim.x, df, outer, total_cap);
 }
 
 // ---- pass B -----------------------------------------------------------------
@@ -305,12 +525,12 @@ __device__ __forceinline__ void pass_b_finish(const Acc& arr, const Acc& arz, do
     }
 }
 
-template <int S, int TJ, bool FIRST>
+template <int S, int TJ, bool FIRST, bool BIN, bool BOUT>
 __device__ __forceinline__ void col_b(const Geo& g, const ColMap& m, const ColCheb& c3, float inv_c0,
                                       const float* __restrict__ r_in, float* __restrict__ r_out,
                                       const float* __restrict__ q, float* __restrict__ z_out, double* partials,
                                       unsigned* counter, SolverState* st, SolverState* outer, int total_cap, int blk,
-                                      int nblk)
+                                      int nblk, const Defer& df)
 {
     constexpr int H = TJ + 2 * S;
     constexpr int NL = S > 1 ? S - 1 : 1;   // stored levels z_1 .. z_{S-1}
@@ -319,8 +539,15 @@ __device__ __forceinline__ void col_b(const Geo& g, const ColMap& m, const ColCh
     const int item = blk * CWPB + (threadIdx.x >> 5);
     const StripPos s = strip_pos<S, TJ>(g, m, item, lane);   // from the arguments only
     dep_wait();
-    if (st->done) return;
-    const float alpha = FIRST ? 0.f : (float)st->alpha;
+    float alpha = 0.f;
+    if (BIN && !FIRST) {   // pass A's sum, alpha (and the commit of the iteration)
+        const HeadOut h = head_b<BOUT>(df.pin, df.nb_in, st, outer, blk);
+        if (h.end) return;
+        alpha = h.coef;
+    } else {
+        if (st->done) return;
+        if (!FIRST) alpha = (float)st->alpha;
+    }
     Acc arr, arz;
     if (item < m.items) {
         float rp[S + 1][H];      // r' at planes I - d
@@ -458,6 +685,11 @@ __device__ __forceinline__ void col_b(const Geo& g, const ColMap& m, const ColCh
         }
     }
     dep_signal();
+    if (BOUT) {
+        Acc v[2] = {arr, arz};
+        put_partials<2>(v, reinterpret_cast<float2*>(sm), df.pout, blk, nblk);
+        return;
+    }
     pass_b_finish<FIRST>(arr, arz, partials, counter, sm, st, outer, total_cap, blk, nblk);
 }
 
@@ -466,10 +698,10 @@ __global__ void __launch_bounds__(CT, (TJ == 4 && S <= 3) ? 3 : 2) k_col_b(Geo g
                                                const float* __restrict__ r_in, float* __restrict__ r_out,
                                                const float* __restrict__ q, float* __restrict__ z_out,
                                                double* partials, unsigned* counter, SolverState* st,
-                                               SolverState* outer, int total_cap)
+                                               SolverState* outer, int total_cap, Defer df)
 {
-    col_b<S, TJ, FIRST>(g, m, c3, inv_c0, r_in, r_out, q, z_out, partials, counter, st, outer, total_cap, blockIdx.x,
-                        gridDim.x);
+    col_b<S, TJ, FIRST, COL_DEFER_AB, COL_DEFER_BA>(g, m, c3, inv_c0, r_in, r_out, q, z_out, partials, counter, st,
+                                                     outer, total_cap, blockIdx.x, gridDim.x, df);
 }
 
 // x += e + alpha p_last (FP64 solution, FP32 correction)
@@ -496,8 +728,9 @@ __global__ void __launch_bounds__(CT, TJ == 8 ? 3 : 2) k_col_a_batch(const Batch
     const int c = batch_case(pre, n, blockIdx.x);
     const BatchCase& C = cs[c];
     const int b0 = __ldg(pre + c), nb = __ldg(pre + c + 1) - b0;
-    col_a<TJ, FIRST>(C.g, C.ma, Coef{C.c0, C.x1, C.y1, C.z1}, C.z, pc ? C.p1 : C.p0, pc ? C.p0 : C.p1, C.q, C.e,
-                     C.partials, C.counters + 15, C.in, pc ^ 1, blockIdx.x - b0, nb);
+    col_a<TJ, FIRST, false, false>(C.g, C.ma, Coef{C.c0, C.x1, C.y1, C.z1}, C.z, pc ? C.p1 : C.p0, pc ? C.p0 : C.p1, C.q,
+                            C.e, C.partials, C.counters + 15, C.in, pc ^ 1, blockIdx.x - b0, nb, Defer{}, C.out,
+                            C.cap);
 }
 
 template <int S, int TJ, bool FIRST>
@@ -508,9 +741,8 @@ __global__ void __launch_bounds__(CT, (TJ == 4 && S <= 3) ? 3 : 2) k_col_b_batch
     const int c = batch_case(pre, n, blockIdx.x);
     const BatchCase& C = cs[c];
     const int b0 = __ldg(pre + c), nb = __ldg(pre + c + 1) - b0;
-    col_b<S, TJ, FIRST>(C.g, C.mb, C.c3, C.inv_c0, rin ? C.r1 : C.r0,
-                        rin ? C.r0 : C.r1, C.q, C.z, C.partials, C.counters + 14, C.in, C.out, C.cap, blockIdx.x - b0,
-                        nb);
+    col_b<S, TJ, FIRST, false, false>(C.g, C.mb, C.c3, C.inv_c0, rin ? C.r1 : C.r0, rin ? C.r0 : C.r1, C.q, C.z, C.partials,
+                               C.counters + 14, C.in, C.out, C.cap, blockIdx.x - b0, nb, Defer{});
 }
 
 // x += e + alpha p_last for the cases in their correction round
@@ -528,9 +760,9 @@ __global__ void k_x_update_batch(const BatchCase* __restrict__ cs, const int* __
 
 // ---- launch plumbing ----------------------------------------------------------
 using KA = void (*)(Geo, ColMap, Coef, const float*, const float*, float*, float*, float*, double*, unsigned*,
-                    SolverState*, int);
+                    SolverState*, int, Defer, SolverState*, int);
 using KB = void (*)(Geo, ColMap, ColCheb, float, const float*, float*, const float*, float*, double*, unsigned*,
-                    SolverState*, SolverState*, int);
+                    SolverState*, SolverState*, int, Defer);
 
 KA pick_a(int tj, bool first)
 {
@@ -652,7 +884,8 @@ les_status col_plan(les_ctx* c, const les_pcg_opts* o, ViewF A, SolverState* in,
     P.mb = col_map(c, (const void*)pick_b(P.S, tjb, false), P.S, tjb, c->tune_cib);
     P.blocks_a = (P.ma.items + CWPB - 1) / CWPB;
     P.blocks_b = (P.mb.items + CWPB - 1) / CWPB;
-    if ((size_t)2 * P.blocks_a > c->partials_len || (size_t)2 * P.blocks_b > c->partials_len)
+    // pass B's partials (2 per block) then pass A's, both live across a pass
+    if ((size_t)2 * P.blocks_b + (size_t)P.blocks_a > c->partials_len)
         return fail(c, LES_BAD_ARG, "column pass grid exceeds the reduction scratch");
     return LES_OK;
 }
@@ -662,8 +895,10 @@ static Coef coef_of(const ColPlan& P) { return Coef{P.A.k.c0, P.A.k.x1, P.A.k.y1
 les_status col_pass_a(les_ctx* c, const ColPlan& P, bool first, int pc)
 {
     float *z = c->f[1], *pb[2] = {c->f[2], c->f[3]}, *q = c->f[4], *e = c->f[5];
+    float2* const part = reinterpret_cast<float2*>(c->partials);   // pass B's pairs, then pass A's
+    const Defer df{part, P.blocks_b, part + 2 * (size_t)P.blocks_b};
     launch_pdl(c, PROF_IN_SPMV, pick_a(P.ma.tj, first), P.blocks_a, CT, c->g, P.ma, coef_of(P), (const float*)z,
-             (const float*)pb[pc], pb[pc ^ 1], q, e, c->partials, c->counters + 15, P.in, pc ^ 1);
+             (const float*)pb[pc], pb[pc ^ 1], q, e, c->partials, c->counters + 15, P.in, pc ^ 1, df, P.out, P.cap);
     return check_launch(c, "column pass A");
 }
 
@@ -671,8 +906,11 @@ les_status col_pass_b(les_ctx* c, const ColPlan& P, bool first, int rin)
 {
     float* r[2] = {c->f[0], c->f[6]};
     float *z = c->f[1], *q = c->f[4];
+    float2* const part = reinterpret_cast<float2*>(c->partials);
+    const Defer df{part + 2 * (size_t)P.blocks_b, P.blocks_a, part};
     launch_pdl(c, PROF_IN_CHEB, pick_b(P.S, P.mb.tj, first), P.blocks_b, CT, c->g, P.mb, P.c3, P.inv_c0,
-             (const float*)r[rin], r[rin ^ 1], (const float*)q, z, c->partials, c->counters + 14, P.in, P.out, P.cap);
+             (const float*)r[rin], r[rin ^ 1], (const float*)q, z, c->partials, c->counters + 14, P.in, P.out, P.cap,
+             df);
     return check_launch(c, "column pass B");
 }
 

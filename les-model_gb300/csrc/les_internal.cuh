@@ -205,6 +205,7 @@ struct SolverState {
     double rho, alpha, beta, err, tol, pq, rr, rz, bnorm, maxdp;
     double scal[8];   // misc scalars (dt, lambda, ...)
     int k, done, iters, max_iter, status, buf, pad0, pad1;
+    double rho_next;  // the column passes' rho, handed from pass A to pass B
 };
 
 // ---- bounded grid barrier for cooperative (co-resident) launches ------------

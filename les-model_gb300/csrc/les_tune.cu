@@ -26,7 +26,7 @@ namespace {
 constexpr int KT = 8;   // timed launches per candidate
 
 // Inputs that keep the passes busy without converging: r = 1, z = 1/2,
-// p = q = e = 0, alpha = beta = 0, rho = 1, tolerance -1 (never met).
+// p = q = e = 0, alpha = beta = 0, tolerance -1 (never met).
 __global__ void k_tune_prep(int n, float* r, float* z, float* p0, float* p1, float* q, float* e, float* r1)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -34,6 +34,14 @@ __global__ void k_tune_prep(int n, float* r, float* z, float* p0, float* p1, flo
     r[t] = 1.f;
     z[t] = 0.5f;
     p0[t] = p1[t] = q[t] = e[t] = r1[t] = 0.f;
+}
+
+// Finite block partials, so that a pass timed on its own (not after the
+// other one) forms finite alpha, beta and residual norms from them.
+__global__ void k_tune_partials(double* p, size_t n)
+{
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) p[t] = 1.0;
 }
 
 __global__ void k_tune_state(SolverState* in, SolverState* out)
@@ -44,7 +52,8 @@ __global__ void k_tune_state(SolverState* in, SolverState* out)
     in->max_iter = 1 << 30;
     in->alpha = 0.0;
     in->beta = 0.0;
-    in->rho = 1.0;
+    in->rho = 1e300;       // beta = r'.z / rho rounds to 0 in FP32: p stays bounded
+    in->rho_next = 1.0;
     in->status = LES_OK;
     out->iters = 0;
 }
@@ -63,6 +72,7 @@ les_status prep(les_ctx* c)
     if (st) return st;
     const int n = c->g.n;
     launch(c, k_tune_prep, (n + 255) / 256, 256, n, c->f[0], c->f[1], c->f[2], c->f[3], c->f[4], c->f[5], c->f[6]);
+    launch(c, k_tune_partials, (unsigned)((c->partials_len + 255) / 256), 256, c->partials, c->partials_len);
     launch(c, k_tune_state, 1, 1, c->state + 1, c->state);
     return check_launch(c, "tune prep");
 }
