@@ -256,6 +256,31 @@ __device__ __forceinline__ void sum_partials(const float2* __restrict__ part, in
     for (int q = 0; q < NV; ++q) v[q] = (double)acc[q].hi + (double)acc[q].lo;
 }
 
+// The last-block form with the same double-float sums: every block leaves
+// its (hi, lo) partials, and the block that arrives last (fence + atomic
+// counter) adds them up; true in every thread of that block, the totals in
+// its thread 0.
+template <int NV>
+__device__ bool last_block_sum_df(Acc (&v)[NV], float2* part, unsigned* counter, float2* sm, int bid, int nb,
+                                  double (&out)[NV])
+{
+    __shared__ int am_last;
+    block_sum_df<NV>(v, sm);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) part[q * nb + bid] = make_float2(v[q].hi, v[q].lo);
+        __threadfence();
+        const unsigned t = atomicAdd(counter, 1u);
+        am_last = t == (unsigned)nb - 1u;
+    }
+    __syncthreads();
+    if (!am_last) return false;
+    __threadfence();
+    sum_partials<NV>(part, nb, out, sm);
+    if (threadIdx.x == 0) *counter = 0u;
+    return true;
+}
+
 // The deferred heads of the two passes, kept out of line: inlined, their
 // FP64 scalars and barriers changed how the march around them was compiled
 // (pass A's march ran 20 % slower).  Both return `end` (leave the kernel:
@@ -475,8 +500,10 @@ __device__ __forceinline__ void col_a(const Geo& g, const ColMap& m, const Coef&
         put_partials<1>(v, reinterpret_cast<float2*>(sm), df.pout, blk, nblk);
         return;
     }
-    double v[1] = {acc_value(acc)};
-    if (last_block_sum<1>(v, partials, counter, sm, blk, nblk)) {
+    Acc va[1] = {acc};
+    double v[1];
+    if (last_block_sum_df<1>(va, reinterpret_cast<float2*>(partials), counter, reinterpret_cast<float2*>(sm), blk,
+                             nblk, v)) {
         if (threadIdx.x == 0) {
             st->alpha = st->rho / v[0];
             st->buf = pslot;   // buffer holding this iteration's p
@@ -503,8 +530,10 @@ __device__ __forceinline__ void pass_b_finish(const Acc& arr, const Acc& arz, do
                                               double* sm, SolverState* st, SolverState* outer, int total_cap,
                                               int blk, int nblk)
 {
-    double v[2] = {acc_value(arr), acc_value(arz)};
-    if (last_block_sum<2>(v, partials, counter, sm, blk, nblk)) {
+    Acc va[2] = {arr, arz};
+    double v[2];
+    if (last_block_sum_df<2>(va, reinterpret_cast<float2*>(partials), counter, reinterpret_cast<float2*>(sm), blk,
+                             nblk, v)) {
         if (threadIdx.x == 0) {
             if (FIRST) {
                 st->rho = v[1];
