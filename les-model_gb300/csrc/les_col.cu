@@ -9,19 +9,23 @@
 // memory and no block barrier inside the march; every warp runs on its own.
 //
 // Pass A (k_col_a), halo 1:
+//     convergence test on ||r'||, beta, rho   (from pass B's sums)
 //     p = z + beta p_old          (strip + halo)
 //     e += alpha_prev p_old       (the previous iteration's update of the inner
 //                                  solution, deferred to here so that pass B
 //                                  reads neither p nor e)
-//     q = A p, p.q -> alpha
+//     q = A p, p.q                (left for pass B)
 // Pass B (k_col_b), halo S:
+//     alpha                       (from pass A's sum)
 //     r' = r - alpha q, ||r'||^2
 //     z = M^-1 r': Chebyshev with S = degree-1 stencil levels (the polynomial
 //       of les-model src/pressure.cpp:871-905 in three-term form, ColCheb),
 //       temporally blocked along i -- at march step I level k works on plane
 //       I-k over the strip grown by S-k cells; Jacobi (S = 0): z = r' / A_c
-//     r'.z -> beta, rho; convergence on ||r'||
-// The last p and alpha of a solve are left for col_x_update (x += e + alpha p).
+//     r'.z                        (left for pass A)
+// The grid sums of one pass are formed by the next (the deferred form below;
+// the batched ensemble kernels reduce at the end of their own pass).  The
+// last p and alpha of a solve are left for col_x_update (x += e + alpha p).
 //
 // Compulsory bytes per cell and iteration: pass A reads z, p_old, e and writes
 // p, q, e (24 B); pass B reads r, q and writes r', z (16 B).
