@@ -248,3 +248,25 @@ def test_tma_fused_matches_plain_fused(shape, pc, deg):
     assert t[1] == f[1] and t[2] == f[2], (t[:4], f[:4])
     assert maxrel(t[4], f[4]) < 1e-12, maxrel(t[4], f[4])
     assert maxrel(t[4], u[4]) < 1e-6, maxrel(t[4], u[4])
+
+
+@pytest.mark.parametrize("cap", [1, 2, 7])
+def test_mixed_column_solve_stops_at_the_iteration_cap(cap):
+    """The register-column passes judge an inner iteration in the pass after
+    it (each pass's grid sums are formed by the next one): a mixed solve
+    capped at `cap` inner iterations must still stop after exactly `cap` of
+    them, report NOT_CONVERGED and leave a finite solution."""
+    m, solid, b = _small_system()
+    tol = 1e-8 * np.linalg.norm(b)
+    with G.Context(m) as c:
+        c.set_option(G.OPT_FUSED, 1)
+        c.upload_mask(np.zeros(m.n, np.uint8))
+        c.build_stencil()
+        lmax = c.lambda_max(20)
+        c.upload("b", b)
+        c.upload("p", np.zeros(m.n))
+        st, r = c.pcg(G.pcg_opts(precond=G.PC_CHEBYSHEV, max_iter=cap, tol=tol, lambda_min=3 * np.pi ** 2,
+                                 lambda_max=lmax, degree=4, precision=G.MIXED, inner_rtol=1e-4))
+        x = c.download("p")
+    assert st == G.NOT_CONVERGED and r.iters == cap, (st, r.iters)
+    assert np.isfinite(r.residual) and np.all(np.isfinite(x))
