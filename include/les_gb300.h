@@ -216,12 +216,14 @@ les_status les_axpby(les_ctx* ctx, int out_slot, double a, int in1_slot, double 
  * a thread that must not take the allocator's locks mid-step.  a, b: device
  * arrays of n doubles; out: device pointer that receives the result; stream:
  * a cudaStream_t (NULL for the default stream); the call is asynchronous on
- * it.  Scratch is a fixed array reserved in device memory when the library is
- * loaded (512 KiB on every device that loads it, held until exit), which caps
- * n at LES_NOALLOC_MAX_CELLS; larger n is rejected with LES_BAD_ARG and a
- * message on stderr.  The first call on a device looks up that array's
- * address (once per device): make that first call before any stream capture.
- * All calls share the scratch, so calls that overlap on the GPU race. */
+ * it.  Scratch is a fixed 512 KiB array in device memory, which caps n at
+ * LES_NOALLOC_MAX_CELLS; larger n is rejected with LES_BAD_ARG and a message
+ * on stderr.  CUDA loads the library's modules lazily, so the array is
+ * reserved on a device by the FIRST call there (which also looks up its
+ * address) and held until the process exits: make that first call during
+ * set-up, before reserving the rest of the device's memory and before any
+ * stream capture; later calls reserve nothing.  All calls share the scratch,
+ * so calls that overlap on the GPU race. */
 #define LES_NOALLOC_MAX_CELLS 134217728LL
 les_status les_dot_noalloc(const double* a, const double* b, long long n, double* out, void* stream);
 
@@ -381,6 +383,11 @@ les_status les_profile(les_ctx* ctx, int enable);
  * (0..7, names from les_profile_name). */
 les_status les_profile_read(les_ctx* ctx, int kernel_id, int* launches, double* total_ms);
 const char* les_profile_name(int kernel_id);
+/* Measured FP64 arithmetic rate of the context's GPU: independent multiply
+ * and add chains (one DMUL + one DADD per a*b+c, as the reference-order FP64
+ * kernels execute them), best of three timed launches; *ops_per_s counts
+ * each multiply and each add.  The denominator of the FP64 path's roofline. */
+les_status les_fp64_rate(les_ctx* ctx, double* ops_per_s);
 /* Records CUDA event slot `mark` (0..63) on the context's stream. */
 les_status les_mark(les_ctx* ctx, int mark);
 /* Device time between two recorded marks, in ms (waits for mark1). */

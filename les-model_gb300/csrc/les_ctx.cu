@@ -101,6 +101,32 @@ static bool mesh_ok(const les_mesh* m)
     return n < (1LL << 31) - 1024;
 }
 
+namespace {
+
+// FP64 pipe probe: independent multiply and add chains (this file is
+// compiled with -fmad=false, so x * a + b is one DMUL and one DADD, the
+// instruction mix of the reference-order FP64 kernels).
+constexpr int FP64_CHAINS = 8;
+constexpr int FP64_ITERS = 4096;
+constexpr int FP64_THREADS = 256;
+
+__global__ void __launch_bounds__(FP64_THREADS) k_fp64_probe(double a, double b, double* sink)
+{
+    double x[FP64_CHAINS];
+#pragma unroll
+    for (int q = 0; q < FP64_CHAINS; ++q) x[q] = (double)(threadIdx.x + q);
+    for (int it = 0; it < FP64_ITERS; ++it) {
+#pragma unroll
+        for (int q = 0; q < FP64_CHAINS; ++q) x[q] = x[q] * a + b;
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int q = 0; q < FP64_CHAINS; ++q) s += x[q];
+    if (s == 1234.5) sink[0] = s;   // keeps the chains live; never true for these inputs
+}
+
+}  // namespace
+
 extern "C" {
 
 int les_abi_version(void) { return LES_ABI_VERSION; }
@@ -190,6 +216,7 @@ void les_destroy(les_ctx* c)
     cudaFree(c->counters);
     cudaFree(c->state);
     cudaFree(c->gsync);
+    cudaFree(c->wave_prog);
     if (c->h_state) cudaFreeHost(c->h_state);
     for (auto& e : c->prof_ev) cudaEventDestroy(e);
     for (auto& e : c->marks) cudaEventDestroy(e);
@@ -457,6 +484,33 @@ const char* les_profile_name(int kernel_id)
     static const char* names[PROF_N] = {"inner_precond_f32", "inner_spmv_f32", "inner_update_f32", "spmv_f64",
                                         "update_f64",     "cheb_f64",       "outer_resid_f64",  "ic_apply"};
     return (kernel_id >= 0 && kernel_id < PROF_N) ? names[kernel_id] : "unknown";
+}
+
+les_status les_fp64_rate(les_ctx* c, double* ops_per_s)
+{
+    if (!c || !ops_per_s) return LES_BAD_ARG;
+    cudaSetDevice(c->device);
+    const int blocks = c->sms * 8;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    les_status st = check_cuda(c, cudaEventCreate(&e0), "cudaEventCreate");
+    if (!st) st = check_cuda(c, cudaEventCreate(&e1), "cudaEventCreate");
+    float best = 0.f;
+    for (int rep = 0; rep < 4 && !st; ++rep) {   // first launch warms up
+        cudaEventRecord(e0, c->stream);
+        k_fp64_probe<<<blocks, FP64_THREADS, 0, c->stream>>>(0.999999, 1e-7, c->partials);
+        ++c->launches;
+        cudaEventRecord(e1, c->stream);
+        st = check_cuda(c, cudaEventSynchronize(e1), "fp64 probe");
+        float t = 0.f;
+        if (!st) st = check_cuda(c, cudaEventElapsedTime(&t, e0, e1), "event time");
+        if (rep > 0 && (best == 0.f || t < best)) best = t;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (st) return st;
+    const double ops = 2.0 * FP64_CHAINS * FP64_ITERS * (double)FP64_THREADS * blocks;
+    *ops_per_s = ops / (best * 1e-3);
+    return LES_OK;
 }
 
 les_status les_get_ic_factor(les_ctx* c, double* const* diag7)

@@ -309,6 +309,12 @@ struct les_ctx {
     les::SolverState* state = nullptr;
     les::SolverState* h_state = nullptr;  // pinned mirror
     unsigned* gsync = nullptr;            // count, gen, error
+    // pipelined wavefronts (les_wavefront.cu): one progress counter per warp
+    // tile, compared against a base that grows from launch to launch (reset
+    // to zero when it nears the int range)
+    int* wave_prog = nullptr;
+    int wave_prog_len = 0;
+    int wave_epoch = 0;
     std::string err;
     // accounting: kernel launches issued by this context, and optional CUDA
     // event timing of the solver's hot kernels (les_profile)

@@ -374,6 +374,13 @@ class Context:
                 out[self.lib.les_profile_name(kid).decode()] = (n, ms)
         return out
 
+    def fp64_rate(self):
+        """Measured FP64 multiply/add rate of the GPU (operations per second)."""
+        r = C.c_double()
+        self.lib.les_fp64_rate.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        self._chk(self.lib.les_fp64_rate(self.h, C.byref(r)))
+        return r.value
+
     # --- autotuner
     def autotune(self, opts, share=1.0):
         """Times strip shapes and chunk lengths of the column passes for opts

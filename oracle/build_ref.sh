@@ -3,9 +3,9 @@
 # its sources where they lie (read-only) together with oracle/ref_harness.cpp.
 # Test infrastructure only: used to generate tests/golden/ and to check the
 # C restatement oracle/les_oracle.c.  Needs the reference checkout; skipped
-# (exit 0, nothing built) when it is absent.
+# (exit 0, nothing built) when REF is unset or holds no sources.
 #
-#   REF=<path to les-model checkout>  (default /root/reference)
+#   REF=<path to a les-model checkout> bash oracle/build_ref.sh
 #
 # Flags follow the reference Makefile (Makefile:2-3: g++ -std=c++17 -O2
 # -fopenmp).  Two additions: -include cstdint, because src/io.cpp uses
@@ -16,9 +16,9 @@
 # GCC would otherwise contract a*b+c).
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
-REF="${REF:-/root/reference}"
-if [ ! -f "$REF/src/pressure.cpp" ]; then
-  echo "build_ref: reference sources not found at $REF; skipping" >&2
+REF="${REF:-}"
+if [ -z "$REF" ] || [ ! -f "$REF/src/pressure.cpp" ]; then
+  echo "build_ref: REF does not name a les-model checkout (REF='$REF'); skipping" >&2
   exit 0
 fi
 mkdir -p "$here/_ref"

@@ -39,9 +39,13 @@ def build_oracle(force=False):
     return ORACLE_SO
 
 
-def build_ref():
-    """Runs oracle/build_ref.sh (no-op without the reference checkout)."""
-    subprocess.check_call(["bash", os.path.join(HERE, "build_ref.sh")])
+def build_ref(ref=None):
+    """Runs oracle/build_ref.sh on the les-model checkout `ref` (default: the
+    REF environment variable; a no-op without a checkout)."""
+    env = dict(os.environ)
+    if ref:
+        env["REF"] = ref
+    subprocess.check_call(["bash", os.path.join(HERE, "build_ref.sh")], env=env)
     return REF_SO if os.path.exists(REF_SO) else None
 
 
@@ -53,6 +57,21 @@ def _p(a):
     assert a.dtype == np.float64 and a.flags.c_contiguous
     return a.ctypes.data_as(_dp)
 
+
+
+def mt19937_start_vector(n, seed=1337):
+    """std::mt19937(seed) + std::uniform_real_distribution<double>(-1, 1) in
+    index order: what src/pressure.cpp:926-931 draws on one thread.  The
+    legacy numpy RandomState seeds MT19937 with the same init_genrand
+    recurrence; generate_canonical<double, 53> combines two 32-bit words as
+    (w0 + w1 * 2^32) / 2^64, and the distribution maps u to (b - a) * u + a."""
+    words = np.random.RandomState(seed).randint(0, 2 ** 32, size=2 * n, dtype=np.uint32)
+    w0 = words[0::2].astype(np.float64)
+    w1 = words[1::2].astype(np.float64)
+    s = w0 + w1 * 4294967296.0
+    u = s / 18446744073709551616.0
+    u = np.where(u >= 1.0, np.nextafter(1.0, 0.0), u)
+    return 2.0 * u + -1.0
 
 class Mesh(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),

@@ -7,8 +7,8 @@ trip), so these vectors are the pin for the oracle and the CUDA path: every
 output below is produced by the reference's own functions, run with one
 OpenMP thread so that reductions are plain left-to-right sums.
 
-Run in a container that has the reference checkout:
-    python oracle/build_ref.sh && python tests/golden/make_golden.py
+Run where a les-model checkout exists, with REF naming it:
+    REF=<checkout> python tests/golden/make_golden.py
 """
 import math
 import os

@@ -9,6 +9,7 @@ import pytest
 from conftest import GRIDS, golden_mesh, load_golden, same
 
 import oracle as O
+from oracle import mt19937_start_vector  # noqa: F401  (also used by the GPU tests)
 
 
 @pytest.fixture(scope="module", params=GRIDS)
@@ -123,21 +124,6 @@ def test_ic(oracle_lib, g):
     z = np.zeros(m.n)
     oracle_lib.ic_apply(m, A, g["in_r"], z)
     assert same(z, g["out_icA_z"])
-
-
-def mt19937_start_vector(n, seed=1337):
-    """std::mt19937(seed) + std::uniform_real_distribution<double>(-1, 1) in
-    index order: what src/pressure.cpp:926-931 draws on one thread.  The
-    legacy numpy RandomState seeds MT19937 with the same init_genrand
-    recurrence; generate_canonical<double, 53> combines two 32-bit words as
-    (w0 + w1 * 2^32) / 2^64, and the distribution maps u to (b - a) * u + a."""
-    words = np.random.RandomState(seed).randint(0, 2 ** 32, size=2 * n, dtype=np.uint32)
-    w0 = words[0::2].astype(np.float64)
-    w1 = words[1::2].astype(np.float64)
-    s = w0 + w1 * 4294967296.0
-    u = s / 18446744073709551616.0
-    u = np.where(u >= 1.0, np.nextafter(1.0, 0.0), u)
-    return 2.0 * u + -1.0
 
 
 def test_lambda_and_chebyshev(oracle_lib, g):

@@ -57,3 +57,51 @@ def test_dot_noalloc_rejects_oversize_and_bad_args():
         assert fn(p, p, 134217728 + 1, p, c.stream) == G.BAD_ARG
         assert fn(p, p, 0, p, c.stream) == G.BAD_ARG
         assert fn(None, p, 10, p, c.stream) == G.BAD_ARG
+
+
+_CHILD = r"""
+import ctypes as C, json, sys
+sys.path[:0] = sys.argv[1:]
+import torch
+import les_gb300 as G
+lib = G.load()
+fn = lib.les_dot_noalloc
+fn.argtypes = [C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p, C.c_void_p]
+fn.restype = C.c_int
+n = 1 << 20
+g = torch.Generator(device="cuda").manual_seed(5)
+a = torch.rand(n, dtype=torch.float64, device="cuda", generator=g) - 0.5
+b = torch.rand(n, dtype=torch.float64, device="cuda", generator=g) - 0.5
+out = torch.zeros(4, dtype=torch.float64, device="cuda")
+want = float(torch.dot(a, b))
+torch.cuda.synchronize()
+free = [torch.cuda.mem_get_info()[0]]
+for q in range(3):
+    st = fn(a.data_ptr(), b.data_ptr(), n, out[q:].data_ptr(), None)
+    assert st == 0, st
+    torch.cuda.synchronize()
+    free.append(torch.cuda.mem_get_info()[0])
+got = [float(x) for x in out[:3].cpu()]
+print(json.dumps({"free": free, "got": got, "want": want}))
+"""
+
+
+def test_dot_noalloc_reserves_nothing_after_its_first_call():
+    """In a fresh process: the first call on the device loads the module that
+    holds the scratch array (CUDA's lazy loading); every later call leaves the
+    device's free memory exactly as it was."""
+    import json
+    import os
+    import subprocess
+    import sys
+
+    here = os.path.dirname(os.path.abspath(__file__))
+    pkg = os.path.join(os.path.dirname(here), "les-model_gb300")
+    r = subprocess.run([sys.executable, "-c", _CHILD, os.path.join(pkg, "py"), pkg], capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    res = json.loads(r.stdout.strip().splitlines()[-1])
+    free = res["free"]
+    assert free[2] == free[1] and free[3] == free[1], free
+    for got in res["got"]:
+        assert abs(got - res["want"]) <= 1e-10 * abs(res["want"]), (got, res["want"])
