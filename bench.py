@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--workload", default="large", choices=("small", "large", "xlarge", "batch", "adjoint"))
     ap.add_argument("--adj-steps", type=int, default=50, help="adjoint workload: forward steps")
     ap.add_argument("--fd-step", type=float, default=1e-6, help="adjoint workload: finite-difference step")
+    ap.add_argument("--adj-tol", type=float, default=1e-12,
+                    help="adjoint workload: relative residual of every forward and adjoint pressure solve")
     ap.add_argument("--batch", type=int, default=64, help="cases of the batch workload")
     ap.add_argument("--ens-batched", type=int, default=1,
                     help="batch workload: 1 the cases' solves in shared kernels, 0 one graph branch per case")
@@ -426,7 +428,7 @@ def run_adjoint(args):
 
     def params(lmax, dt, cs):
         return G.step_params(nu=les_cases.NU, rho=les_cases.RHO, cs=cs, dt_fixed=dt, solver=G.SOLVER_PCG,
-                             rel_tol=1e-12,
+                             rel_tol=args.adj_tol,
                              pcg=G.pcg_opts(precond=G.PC_CHEBYSHEV, max_iter=50000, lambda_min=3 * np.pi ** 2,
                                             lambda_max=lmax, degree=4, precision=G.MIXED, inner_rtol=1e-4))
 
@@ -435,14 +437,14 @@ def run_adjoint(args):
     def J_of(prof, cs):
         with G.Context(mesh) as c:
             lmax, dt = setup(c, prof)
-            return c.adjoint_forward(params(lmax, dt, cs), nsteps, 10, box, 1e-12)
+            return c.adjoint_forward(params(lmax, dt, cs), nsteps, 10, box, args.adj_tol)
 
     with G.Context(mesh) as c:
         lmax, dt = setup(c, prof0)
         prm = params(lmax, dt, les_cases.CS)
         c.sync()
         t0 = time.perf_counter()
-        J = c.adjoint_forward(prm, nsteps, 10, box, 1e-12)
+        J = c.adjoint_forward(prm, nsteps, 10, box, args.adj_tol)
         t_fwd = time.perf_counter() - t0
         t0 = time.perf_counter()
         g, gcs = c.adjoint_backward()
@@ -474,7 +476,7 @@ def run_adjoint(args):
     errs = [r["rel_err"] for r in rows] + [cs_err]
     line = {"metric": "adjoint gradient of the probe-box kinetic energy vs central finite differences",
             "value": max(errs), "unit": "max relative error", "higher_is_better": False, "n_gpus": 1,
-            "steps": nsteps, "warmup": 0, "dtype": "f32 inner / f64 outer (tol 1e-12)", "data": "synthetic",
+            "steps": nsteps, "warmup": 0, "dtype": "f32 inner / f64 outer (tol %g)" % args.adj_tol, "data": "synthetic",
             "config": {"workload": "adjoint 128x64x64 h=1/64 centred cube, %d steps, dt %.3g fixed, checkpoint "
                                    "every 10, probe [96,120)x[16,48)x[16,48), controls 64x64 inlet u + Cs" % (nsteps, dt),
                        "fd_step": hs, "fd_entries": 16},

@@ -31,6 +31,7 @@ using namespace les;
 namespace les {
 les_status ensure_stored_A(les_ctx* c);
 les_status ic_apply_dev32(les_ctx* c, const float* r, float* z, const float* const* L32, SolverState* st);
+les_status wave_check(les_ctx* c);
 }
 
 namespace {
@@ -499,6 +500,10 @@ les_status pcg_mixed_impl(les_ctx* c, const les_pcg_opts* o, les_pcg_result* res
         st = read_state(c);
         if (st) return st;
         if (c->h_state[1].status == LES_NONFINITE) break;
+    }
+    if (mode == 2) {   // the IC wavefront's bounded waits
+        st = wave_check(c);
+        if (st) return st;
     }
     const SolverState& h = c->h_state[0];
     if (res) {

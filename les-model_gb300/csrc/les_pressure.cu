@@ -21,6 +21,7 @@ using namespace les;
 
 namespace les {
 les_status ic_apply_dev(les_ctx* c, const double* r, double* z, const double* const* Lsrc, int skip_done);
+les_status wave_check(les_ctx* c);
 les_status build_ic_dev(les_ctx* c);
 les_status pcg_mixed(les_ctx* c, const les_pcg_opts* o, les_pcg_result* res);
 }
@@ -652,6 +653,10 @@ les_status pcg_fp64(les_ctx* c, const les_pcg_opts* o, les_pcg_result* res, int 
         batch = batch < 32 ? batch * 2 : 32;
         if (launched + batch > o->max_iter + 1) batch = o->max_iter + 1 - launched;
         if (batch < 1) batch = 1;
+    }
+    if (o->precond == LES_PC_IC || o->precond == LES_PC_IC_A) {   // the wavefront's bounded waits
+        st = wave_check(c);
+        if (st) return st;
     }
     const SolverState& h = *c->h_state;
     if (res) {

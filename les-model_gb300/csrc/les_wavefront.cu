@@ -4,17 +4,29 @@
 // (:212-246).
 //
 // Each cell of these loops depends only on its (i-1), (j-1), (k-1)
-// neighbours (the backward solve: on i+1, j+1, k+1), so all cells on one
-// hyperplane i+j+k = s can be processed at once, and processing hyperplanes in
-// order s = 0, 1, 2, ... performs exactly the same floating-point operations
-// on exactly the same operand values as the serial lexicographic loop.  The
-// result is therefore bit-identical to the reference.
+// neighbours (the backward solve: on i+1, j+1, k+1), so any order that
+// computes a cell after those neighbours performs exactly the same
+// floating-point operations on exactly the same operand values as the serial
+// lexicographic loop: the results are bit-identical to the reference.
 //
-// Hyperplanes run inside one cooperative (co-resident) persistent kernel,
-// separated by a grid barrier whose waits are bounded (les_internal.cuh); a
-// timed-out wait sets an error flag, every block leaves, and the host reports
-// LES_TIMEOUT.  Neighbour values written by other blocks are read through L2
-// (__ldcg).  Compiled with -fmad=false.
+// The substitution and the SOR sweep run as a pipelined wavefront with no
+// grid barrier inside a sweep.  The (j, k) plane is cut into warp tiles of TJ
+// rows by 32 columns; a warp owns a tile and marches along i.  Lane l works
+// on plane i = tau - l at its step tau (the lanes are skewed by one plane), so
+// the k-1 neighbour of a cell is lane l-1's result of the step before (a warp
+// shuffle), the j-1 neighbour is the row before in the same thread, and the
+// i-1 neighbour is the thread's own result of the step before.  Only a tile's
+// first row and its first lane need values of other tiles: the tile below in
+// j and the tile before in k publish their progress (steps completed, one
+// counter per tile, release store after a fence) every WB steps, and a warp
+// waits (acquire load, bounded by %globaltimer) for the progress its next WB
+// steps need, then reads those neighbours through L2.  The backward solve
+// mirrors every direction.  Tiles are handed out to the resident warps in an
+// order in which each tile's producers come first, so the waits always end.
+// The IC factorisation (set-up, once) keeps the simpler form: hyperplanes
+// i+j+k = s in order, one grid barrier between them.  Every wait is bounded
+// (about 2 s); a wait that gives up sets an error flag, every warp leaves,
+// and the host reports LES_TIMEOUT.  Compiled with -fmad=false.
 #include <cmath>
 
 #include "les_internal.cuh"
@@ -65,139 +77,399 @@ __global__ void k_ic_build(Plane P, StencilView A, double* Lc, double* Lw, doubl
     }
 }
 
-// apply_ic_preconditioner, src/pressure.cpp:442-482: forward substitution in
-// increasing hyperplane order, then backward substitution in decreasing order.
-// T = double is the reference's arithmetic; T = float serves the FP32 inner
-// solve of the mixed-precision path (st == nullptr: never skipped).
-template <typename T>
-__global__ void k_ic_apply(Plane P, const T* __restrict__ Lc, const T* __restrict__ Lw,
-                           const T* __restrict__ Ls, const T* __restrict__ Lb,
-                           const T* __restrict__ r, T* z, GridSync gs, const SolverState* st,
-                           int skip_done)
+// ---- pipelined wavefront -----------------------------------------------------
+constexpr int WB = 8;          // steps between progress publications
+constexpr int WAVE_TJ = 4;     // rows per warp tile
+
+struct Wave {
+    int nx, ny, nz, si, sj;    // the swept box (interior for GS-SOR) and the strides
+    int off;                   // index of the box's first cell
+    int wj, wk, ntiles;        // warp tiles along j and k
+    int steps;                 // marching steps of a tile: planes + 31
+    int* prog;                 // progress counter per tile
+    int* err;                  // set by a wait that gives up
+};
+
+__device__ __forceinline__ int ld_acquire(const int* p)
 {
-    if (skip_done && st && st->done) return;   // uniform across blocks: no barrier is entered
-    const int smax = P.nx + P.ny + P.nz - 3;
-    const int njk = P.ny * P.nz;
-    for (int s = 0; s <= smax; ++s) {
-        for (int t = gtid(); t < njk; t += gthreads()) {
-            int j = t / P.nz, k = t - j * P.nz;
-            int i = s - j - k;
-            if (i < 0 || i >= P.nx) continue;
-            int id = i * P.si + j * P.sj + k;
-            T sum = r[id];
-            if (i > 0) sum -= Lw[id] * __ldcg(z + id - P.si);
-            if (j > 0) sum -= Ls[id] * __ldcg(z + id - P.sj);
-            if (k > 0) sum -= Lb[id] * __ldcg(z + id - 1);
-            z[id] = sum / Lc[id];
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(int* p, int v)
+{
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Lane 0: waits until *p has reached target (wrap-safe); false once the wait
+// gave up (~2 s) or another warp raised the error flag.
+__device__ bool wait_progress(const int* p, int target, int* err)
+{
+    if (ld_acquire(p) - target >= 0) return true;
+    const unsigned long long t0 = globaltimer_ns();
+    unsigned spins = 0;
+    for (;;) {
+        if (ld_acquire(p) - target >= 0) return true;
+        if (*(volatile int*)err) return false;
+        if ((++spins & 63u) == 0u && globaltimer_ns() - t0 > 2000000000ull) {
+            atomicExch(err, 1);
+            return false;
         }
-        if (!grid_barrier(gs)) return;
-    }
-    for (int s = smax; s >= 0; --s) {
-        for (int t = gtid(); t < njk; t += gthreads()) {
-            int j = t / P.nz, k = t - j * P.nz;
-            int i = s - j - k;
-            if (i < 0 || i >= P.nx) continue;
-            int id = i * P.si + j * P.sj + k;
-            T sum = __ldcg(z + id);
-            if (i < P.nx - 1) sum -= Lw[id + P.si] * __ldcg(z + id + P.si);
-            if (j < P.ny - 1) sum -= Ls[id + P.sj] * __ldcg(z + id + P.sj);
-            if (k < P.nz - 1) sum -= Lb[id + 1] * __ldcg(z + id + 1);
-            z[id] = sum / Lc[id];
-        }
-        if (!grid_barrier(gs)) return;
+        __nanosleep(32);
     }
 }
 
-// solve_pressure_GS, src/pressure.cpp:212-246: up to max_iter SOR sweeps over
-// the interior in hyperplane order, each followed by apply_pressure_BCs
-// (face closed form, then the obstacle copy) and the max|dp| < tol test.
-__global__ void k_gs_sor(Plane P, double dx2, double dy2, double dz2, double omega, double coef,
-                         double tol, int max_iter, const double* __restrict__ rhs, double* p,
-                         const uint8_t* __restrict__ solid, const int* __restrict__ solid_list,
-                         int n_solid, double* block_max, SolverState* st, GridSync gs)
+// Max over the warp, the same value in every lane.
+__device__ __forceinline__ double warp_max_all(double v)
 {
-    __shared__ double smax_w[32];
-    const int nyi = P.ny - 2, nzi = P.nz - 2;
-    const int njk = nyi * nzi;
-    const int s_lo = 3, s_hi = (P.nx - 2) + (P.ny - 2) + (P.nz - 2);
-    const int nfaces_i = P.ny * P.nz;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Publishes `value` as the tile's progress after every lane's stores.
+__device__ __forceinline__ void publish(int* p, int value)
+{
+    __threadfence();
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) st_release(p, value);
+}
+
+// Tile t's producers: DIR > 0 the tiles below in j (t-1) and before in k
+// (t-wj); DIR < 0 the tiles above (t+1) and after (t+wj).
+struct TileDeps {
+    int dj, dk;
+};
+
+template <int DIR>
+__device__ __forceinline__ TileDeps tile_deps(const Wave& W, int J, int K, int t)
+{
+    TileDeps d;
+    if (DIR > 0) {
+        d.dj = J > 0 ? t - 1 : -1;
+        d.dk = K > 0 ? t - W.wj : -1;
+    } else {
+        d.dj = J < W.wj - 1 ? t + 1 : -1;
+        d.dk = K < W.wk - 1 ? t + W.wj : -1;
+    }
+    return d;
+}
+
+// Waits for the progress a batch of steps [tau0, tend) needs: the j-producer
+// must have completed those steps, the k-producer 31 more (its far lane
+// reaches a plane 31 steps after its near lane).  Returns false in every lane
+// when a wait gave up.
+__device__ __forceinline__ bool wait_batch(const Wave& W, const TileDeps& d, int base, int tend)
+{
+    int ok = 1;
+    if ((threadIdx.x & 31) == 0) {
+        if (d.dj >= 0 && !wait_progress(W.prog + d.dj, base + tend, W.err)) ok = 0;
+        if (ok && d.dk >= 0 && !wait_progress(W.prog + d.dk, base + min(tend + 31, W.steps), W.err)) ok = 0;
+    }
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    __syncwarp();
+    return ok != 0;
+}
+
+// IC(0) substitution of one tile, src/pressure.cpp:442-482.  DIR > 0: the
+// forward solve L y = r (z = y); DIR < 0: the backward solve L^T z = y.
+// Row r of the tile is grid row j = jb + r (forward) or jb + rows-1-r
+// (backward); lane l is column k = K*32 + l and starts plane i after
+// skew(l) steps (l forward, 31-l backward).
+template <typename T, int DIR>
+__device__ bool ic_tile(const Wave& W, int t, int base, const T* __restrict__ Lc, const T* __restrict__ Lw,
+                        const T* __restrict__ Ls, const T* __restrict__ Lb, const T* __restrict__ r, T* z)
+{
+    constexpr int TJ = WAVE_TJ;
+    constexpr unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int J = t % W.wj, K = t / W.wj;
+    const int jb = J * TJ, rows = min(TJ, W.ny - jb);
+    const int k = K * 32 + lane;
+    const bool kin = k < W.nz;
+    const int sk = DIR > 0 ? lane : 31 - lane;
+    const TileDeps d = tile_deps<DIR>(W, J, K, t);
+    const int jn = DIR > 0 ? jb - 1 : jb + rows;              // neighbour row of row 0
+    const int kn = DIR > 0 ? K * 32 - 1 : K * 32 + 32;        // neighbour column of the near lane
+    const int near = DIR > 0 ? 0 : 31;                        // lane that reads the k-producer
+    auto jrow = [&](int q) { return DIR > 0 ? jb + q : jb + rows - 1 - q; };
+    auto plane = [&](int tau, int skew) { return DIR > 0 ? tau - skew : W.nx - 1 - (tau - skew); };
+    T prev[TJ], outp[TJ];
+#pragma unroll
+    for (int q = 0; q < TJ; ++q) prev[q] = outp[q] = T(0);
+    for (int tau0 = 0; tau0 < W.steps; tau0 += WB) {
+        const int tend = min(tau0 + WB, W.steps);
+        if (!wait_batch(W, d, base, tend)) return false;
+        // the batch's cross-tile neighbours, through L2: the j-neighbour of
+        // row 0 for every step (own column), and the k-neighbours of the near
+        // lane (lane q holds those of step tau0 + q)
+        T zj[WB], zk0[TJ];
+#pragma unroll
+        for (int q = 0; q < WB; ++q) {
+            const int i = plane(tau0 + q, sk);
+            zj[q] = (d.dj >= 0 && kin && tau0 + q < tend && i >= 0 && i < W.nx)
+                        ? __ldcg(z + W.off + i * W.si + jn * W.sj + k) : T(0);
+        }
+        {
+            const int i = plane(tau0 + lane, 0);
+            const bool ok = d.dk >= 0 && lane < WB && tau0 + lane < tend && i >= 0 && i < W.nx;
+#pragma unroll
+            for (int q = 0; q < TJ; ++q)
+                zk0[q] = (ok && q < rows) ? __ldcg(z + W.off + i * W.si + jrow(q) * W.sj + kn) : T(0);
+        }
+#pragma unroll
+        for (int q = 0; q < WB; ++q) {
+            const int tau = tau0 + q;
+            if (tau >= tend) break;   // warp-uniform
+            const int i = plane(tau, sk);
+            const bool act = kin && i >= 0 && i < W.nx;
+            T zk[TJ];
+#pragma unroll
+            for (int s2 = 0; s2 < TJ; ++s2) {
+                zk[s2] = DIR > 0 ? __shfl_up_sync(FULL, outp[s2], 1) : __shfl_down_sync(FULL, outp[s2], 1);
+                const T v = __shfl_sync(FULL, zk0[s2], q);
+                if (lane == near) zk[s2] = v;
+            }
+            T out[TJ];
+#pragma unroll
+            for (int s2 = 0; s2 < TJ; ++s2) {
+                out[s2] = T(0);
+                if (act && s2 < rows) {
+                    const int j = jrow(s2);
+                    const int id = W.off + i * W.si + j * W.sj + k;
+                    const T zjv = s2 == 0 ? zj[q] : out[s2 - 1];
+                    T sum;
+                    if (DIR > 0) {   // :451-463
+                        sum = r[id];
+                        if (i > 0) sum -= Lw[id] * prev[s2];
+                        if (j > 0) sum -= Ls[id] * zjv;
+                        if (k > 0) sum -= Lb[id] * zk[s2];
+                    } else {         // :469-481
+                        sum = __ldcg(z + id);
+                        if (i < W.nx - 1) sum -= Lw[id + W.si] * prev[s2];
+                        if (j < W.ny - 1) sum -= Ls[id + W.sj] * zjv;
+                        if (k < W.nz - 1) sum -= Lb[id + 1] * zk[s2];
+                    }
+                    out[s2] = sum / Lc[id];
+                    z[id] = out[s2];
+                }
+            }
+#pragma unroll
+            for (int s2 = 0; s2 < TJ; ++s2) prev[s2] = outp[s2] = out[s2];
+        }
+        publish(W.prog + t, base + tend);
+    }
+    return true;
+}
+
+// apply_ic_preconditioner, src/pressure.cpp:442-482: the forward solve over
+// all tiles, one grid barrier, the backward solve.  T = double is the
+// reference's arithmetic; T = float serves the FP32 inner solve of the
+// mixed-precision path (st == nullptr: never skipped).
+template <typename T>
+__global__ void __launch_bounds__(32) k_ic_wave(Wave W, int base, const T* __restrict__ Lc, const T* __restrict__ Lw,
+                                                const T* __restrict__ Ls, const T* __restrict__ Lb,
+                                                const T* __restrict__ r, T* z, GridSync gs, const SolverState* st,
+                                                int skip_done)
+{
+    if (skip_done && st && st->done) return;   // uniform across blocks: no barrier is entered
+    const int w = blockIdx.x, nw = gridDim.x;  // one warp per block
+    bool ok = true;
+    for (int t = w; t < W.ntiles && ok; t += nw) ok = ic_tile<T, 1>(W, t, base, Lc, Lw, Ls, Lb, r, z);
+    if (!grid_barrier(gs) || !ok) return;
+    for (int t = w; t < W.ntiles && ok; t += nw)
+        ok = ic_tile<T, -1>(W, W.ntiles - 1 - t, base + W.steps + 1, Lc, Lw, Ls, Lb, r, z);
+}
+
+// One lexicographic SOR sweep of one tile over the interior, :216-234:
+// p = (1-omega) p + omega coef ((p_e + p_w)/dx2 + (p_n + p_s)/dy2 + (p_t + p_b)/dz2 - rhs)
+// with the west, south and bottom neighbours already updated in this sweep
+// and the east, north and top ones not yet.  POW2: dx2, dy2, dz2 are powers
+// of two, so x / d2 is exactly x * (1 / d2) and the divisions become
+// multiplications (same results bit for bit).  Returns the tile's max |dp| in
+// *res (per lane).
+template <bool POW2>
+__device__ bool gs_tile(const Wave& W, int t, int base, double d2x, double d2y, double d2z, double one_m_omega,
+                        double omega_coef, const double* __restrict__ rhs, double* p, double& maxr)
+{
+    constexpr int TJ = WAVE_TJ;
+    constexpr unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int J = t % W.wj, K = t / W.wj;
+    const int jb = J * TJ, rows = min(TJ, W.ny - jb);
+    const int k = K * 32 + lane;   // interior coordinates: grid cell (i+1, j+1, k+1)
+    const bool kin = k < W.nz;
+    const TileDeps d = tile_deps<1>(W, J, K, t);
+    const int ssi = W.si, ssj = W.sj;
+    double prev[TJ], outp[TJ];
+#pragma unroll
+    for (int q = 0; q < TJ; ++q) prev[q] = outp[q] = 0.0;
+    auto div2 = [&](double x, double dd) { return POW2 ? x * dd : x / dd; };
+    // Old values a step reads -- its cells and their east, north and top
+    // neighbours, and rhs -- are fetched one step ahead, before the current
+    // step writes: those cells are written only at later steps (the cell by
+    // this lane at its step, the top neighbour by the next lane one step
+    // later, the row above by the tile above, which waits for this one).
+    struct Old {
+        double po[TJ], pe[TJ], pt[TJ], rh[TJ], pw[TJ], pn;
+    };
+    auto fetch = [&](int tau, Old& o) {
+        const int i = tau - lane;
+        const bool act = kin && i >= 0 && i < W.nx;
+#pragma unroll
+        for (int s2 = 0; s2 < TJ; ++s2) {
+            const int id = W.off + i * ssi + (jb + s2) * ssj + k;
+            const bool a = act && s2 < rows;
+            o.po[s2] = a ? __ldcg(p + id) : 0.0;
+            o.pe[s2] = a ? __ldcg(p + id + ssi) : 0.0;
+            o.pt[s2] = a ? __ldcg(p + id + 1) : 0.0;
+            o.rh[s2] = a ? rhs[id] : 0.0;
+            o.pw[s2] = (a && i == 0) ? __ldcg(p + id - ssi) : 0.0;   // plane i = 0: the inlet face
+        }
+        o.pn = act ? __ldcg(p + W.off + i * ssi + (jb + rows) * ssj + k) : 0.0;
+    };
+    Old nx_old;
+    fetch(0, nx_old);
+    for (int tau0 = 0; tau0 < W.steps; tau0 += WB) {
+        const int tend = min(tau0 + WB, W.steps);
+        if (!wait_batch(W, d, base, tend)) return false;
+        // the row below the tile (updated by the tile below, or the wall row
+        // j = 0) for every step, and the column before the near lane's (the
+        // tile before in k, or the wall column k = 0) for the batch
+        double ps0[WB], pb0[TJ];
+#pragma unroll
+        for (int q = 0; q < WB; ++q) {
+            const int i = tau0 + q - lane;
+            ps0[q] = (kin && tau0 + q < tend && i >= 0 && i < W.nx)
+                         ? __ldcg(p + W.off + i * ssi + (jb - 1) * ssj + k) : 0.0;
+        }
+        {
+            const int i = tau0 + lane;
+            const bool ok = lane < WB && tau0 + lane < tend && i >= 0 && i < W.nx;
+#pragma unroll
+            for (int q = 0; q < TJ; ++q)
+                pb0[q] = (ok && q < rows) ? __ldcg(p + W.off + i * ssi + (jb + q) * ssj + K * 32 - 1) : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < WB; ++q) {
+            const int tau = tau0 + q;
+            if (tau >= tend) break;   // warp-uniform
+            const int i = tau - lane;
+            const bool act = kin && i >= 0 && i < W.nx;
+            const Old o = nx_old;
+            if (tau + 1 < W.steps) fetch(tau + 1, nx_old);
+            double pb[TJ];
+#pragma unroll
+            for (int s2 = 0; s2 < TJ; ++s2) {
+                pb[s2] = __shfl_up_sync(FULL, outp[s2], 1);
+                const double v = __shfl_sync(FULL, pb0[s2], q);
+                if (lane == 0) pb[s2] = v;
+            }
+            double out[TJ];
+#pragma unroll
+            for (int s2 = 0; s2 < TJ; ++s2) {
+                out[s2] = 0.0;
+                if (act && s2 < rows) {
+                    const int id = W.off + i * ssi + (jb + s2) * ssj + k;
+                    const double pw = i == 0 ? o.pw[s2] : prev[s2];
+                    const double ps = s2 == 0 ? ps0[q] : out[s2 - 1];
+                    const double pn = s2 + 1 < rows ? o.po[s2 + 1] : o.pn;
+                    const double v = one_m_omega * o.po[s2] +
+                                     omega_coef * ((div2(o.pe[s2] + pw, d2x) + div2(pn + ps, d2y)) +
+                                                   div2(o.pt[s2] + pb[s2], d2z) - o.rh[s2]);
+                    p[id] = v;
+                    out[s2] = v;
+                    const double res = fabs(v - o.po[s2]);
+                    if (res > maxr) maxr = res;
+                }
+            }
+#pragma unroll
+            for (int s2 = 0; s2 < TJ; ++s2) prev[s2] = outp[s2] = out[s2];
+        }
+        publish(W.prog + t, base + tend);
+    }
+    return true;
+}
+
+// solve_pressure_GS, src/pressure.cpp:212-246: up to max_iter SOR sweeps over
+// the interior, each a pipelined wavefront followed by apply_pressure_BCs
+// (face closed form, then the obstacle copy) and the max|dp| < tol test.
+template <bool POW2>
+__global__ void __launch_bounds__(32) k_gs_wave(Wave W, int base, double d2x, double d2y, double d2z, double omega,
+                                                double coef, double tol, int max_iter,
+                                                const double* __restrict__ rhs, double* p,
+                                                const uint8_t* __restrict__ solid, const int* __restrict__ solid_list,
+                                                int n_solid, double* block_max, SolverState* st, GridSync gs,
+                                                int nx, int ny, int nz)
+{
+    const int w = blockIdx.x, nw = gridDim.x;   // one warp per block
+    const int lane = threadIdx.x & 31;
+    const int gt = w * 32 + lane, gn = nw * 32;
     const double one_m_omega = 1 - omega;
     const double omega_coef = omega * coef;
+    const int si = ny * nz, sj = nz;
+    const int nfaces_i = ny * nz;
     int sweeps = 0;
     bool converged = false;
     for (int iter = 0; iter < max_iter; ++iter) {
-        double lmax = 0.0;
-        for (int s = s_lo; s <= s_hi; ++s) {
-            for (int t = gtid(); t < njk; t += gthreads()) {
-                int jj = t / nzi, kk = t - jj * nzi;
-                int j = jj + 1, k = kk + 1;
-                int i = s - j - k;
-                if (i < 1 || i > P.nx - 2) continue;
-                int id = i * P.si + j * P.sj + k;
-                double p_old = __ldcg(p + id);
-                double v = one_m_omega * p_old +
-                           omega_coef * ((__ldcg(p + id + P.si) + __ldcg(p + id - P.si)) / dx2 +
-                                         (__ldcg(p + id + P.sj) + __ldcg(p + id - P.sj)) / dy2 +
-                                         (__ldcg(p + id + 1) + __ldcg(p + id - 1)) / dz2 - rhs[id]);
-                p[id] = v;
-                double res = fabs(v - p_old);
-                if (res > lmax) lmax = res;
-            }
-            if (!grid_barrier(gs)) return;
-        }
+        double maxr = 0.0;
+        bool ok = true;
+        const int b = base + iter * (W.steps + 1);
+        for (int t = w; t < W.ntiles && ok; t += nw)
+            ok = gs_tile<POW2>(W, t, b, d2x, d2y, d2z, one_m_omega, omega_coef, rhs, p, maxr);
+        if (!grid_barrier(gs) || !ok) return;
         // apply_pressure_BCs faces: every face cell from interior values
         {
-            const int nface = 2 * nfaces_i + 2 * (P.nx - 2) * P.nz + 2 * (P.nx - 2) * (P.ny - 2);
-            for (int t = gtid(); t < nface; t += gthreads()) {
+            const int nface = 2 * nfaces_i + 2 * (nx - 2) * nz + 2 * (nx - 2) * (ny - 2);
+            for (int q = gt; q < nface; q += gn) {
                 int i, j, k;
-                if (t < 2 * nfaces_i) {
-                    int q = t % nfaces_i;
-                    i = (t < nfaces_i) ? 0 : P.nx - 1;
-                    j = q / P.nz; k = q - j * P.nz;
-                } else if (t < 2 * nfaces_i + 2 * (P.nx - 2) * P.nz) {
-                    int q = t - 2 * nfaces_i, half = (P.nx - 2) * P.nz;
-                    j = (q < half) ? 0 : P.ny - 1;
-                    q = q % half;
-                    i = 1 + q / P.nz; k = q % P.nz;
+                if (q < 2 * nfaces_i) {
+                    const int e = q % nfaces_i;
+                    i = (q < nfaces_i) ? 0 : nx - 1;
+                    j = e / nz; k = e - j * nz;
+                } else if (q < 2 * nfaces_i + 2 * (nx - 2) * nz) {
+                    int e = q - 2 * nfaces_i;
+                    const int half = (nx - 2) * nz;
+                    j = (e < half) ? 0 : ny - 1;
+                    e = e % half;
+                    i = 1 + e / nz; k = e % nz;
                 } else {
-                    int q = t - 2 * nfaces_i - 2 * (P.nx - 2) * P.nz, half = (P.nx - 2) * (P.ny - 2);
-                    k = (q < half) ? 0 : P.nz - 1;
-                    q = q % half;
-                    i = 1 + q / (P.ny - 2); j = 1 + q % (P.ny - 2);
+                    int e = q - 2 * nfaces_i - 2 * (nx - 2) * nz;
+                    const int half = (nx - 2) * (ny - 2);
+                    k = (e < half) ? 0 : nz - 1;
+                    e = e % half;
+                    i = 1 + e / (ny - 2); j = 1 + e % (ny - 2);
                 }
-                int id = i * P.si + j * P.sj + k;
-                if (i == P.nx - 1) { p[id] = 0.0; continue; }
-                int jc = j < 1 ? 1 : (j > P.ny - 2 ? P.ny - 2 : j);
-                int kc = k < 1 ? 1 : (k > P.nz - 2 ? P.nz - 2 : k);
-                int ic = i == 0 ? 1 : i;
-                p[id] = __ldcg(p + ic * P.si + jc * P.sj + kc);
+                const int id = i * si + j * sj + k;
+                if (i == nx - 1) { p[id] = 0.0; continue; }
+                const int jc = j < 1 ? 1 : (j > ny - 2 ? ny - 2 : j);
+                const int kc = k < 1 ? 1 : (k > nz - 2 ? nz - 2 : k);
+                const int ic = i == 0 ? 1 : i;
+                p[id] = __ldcg(p + ic * si + jc * sj + kc);
             }
         }
         if (!grid_barrier(gs)) return;
-        for (int t = gtid(); t < n_solid; t += gthreads()) {
-            const int id = solid_list[t];
-            if (!solid[id + P.si]) p[id] = __ldcg(p + id + P.si);
-            else if (!solid[id - P.si]) p[id] = __ldcg(p + id - P.si);
-            else if (!solid[id + P.sj]) p[id] = __ldcg(p + id + P.sj);
-            else if (!solid[id - P.sj]) p[id] = __ldcg(p + id - P.sj);
+        for (int q = gt; q < n_solid; q += gn) {
+            const int id = solid_list[q];
+            if (!solid[id + si]) p[id] = __ldcg(p + id + si);
+            else if (!solid[id - si]) p[id] = __ldcg(p + id - si);
+            else if (!solid[id + sj]) p[id] = __ldcg(p + id + sj);
+            else if (!solid[id - sj]) p[id] = __ldcg(p + id - sj);
             else if (!solid[id + 1]) p[id] = __ldcg(p + id + 1);
             else if (!solid[id - 1]) p[id] = __ldcg(p + id - 1);
         }
-        // block max -> global max (exact), identical in every block
-        lmax = warp_max(lmax);
-        if ((threadIdx.x & 31) == 0) smax_w[threadIdx.x >> 5] = lmax;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double m = 0.0;
-            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) m = fmax(m, smax_w[q]);
-            block_max[blockIdx.x] = m;
-        }
+        // warp max -> global max (exact), identical in every lane of every
+        // warp (a butterfly, so that the break below is uniform)
+        maxr = warp_max_all(maxr);
+        if (lane == 0) block_max[w] = maxr;
         if (!grid_barrier(gs)) return;
         double gmax = 0.0;
-        for (int b = 0; b < (int)gridDim.x; ++b) gmax = fmax(gmax, __ldcg(block_max + b));
+        for (int q = lane; q < nw; q += 32) gmax = fmax(gmax, __ldcg(block_max + q));
+        gmax = warp_max_all(gmax);
         sweeps = iter + 1;
         if (gmax < tol) { converged = true; break; }
-        // block_max is rewritten next sweep only after the hyperplane barriers
+        // block_max is rewritten next sweep only after the sweep's barrier
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         st->iters = sweeps;
@@ -230,7 +502,8 @@ les_status coop_launch(les_ctx* c, const void* fn, void** args, int* grid_out, i
     if (per_sm < 1) return fail(c, LES_CUDA_ERROR, "wavefront kernel cannot be resident");
     int grid = c->sms;   // one block per SM: enough threads for the widest hyperplane
     if (grid_out) *grid_out = grid;
-    st = check_cuda(c, cudaMemsetAsync(c->gsync, 0, sizeof(unsigned) * 4, c->stream), "reset barrier");
+    // count and generation only: the error word stays set until the host reads it
+    st = check_cuda(c, cudaMemsetAsync(c->gsync, 0, sizeof(unsigned) * 2, c->stream), "reset barrier");
     if (st) return st;
     cudaEvent_t e1 = nullptr;
     if (pid >= 0 && c->prof_on) prof_begin(c, pid, &e1);
@@ -259,35 +532,115 @@ les_status check_barrier(les_ctx* c)
     if (st) return st;
     st = check_cuda(c, cudaStreamSynchronize(c->stream), "sync");
     if (st) return st;
-    if (h[2]) return fail(c, LES_TIMEOUT, "a wavefront grid barrier timed out");
+    if (h[2]) {
+        st = check_cuda(c, cudaMemsetAsync(c->gsync + 2, 0, sizeof(unsigned), c->stream), "clear error");
+        if (st) return st;
+        return fail(c, LES_TIMEOUT, "a bounded wavefront wait timed out");
+    }
     return LES_OK;
+}
+
+// The warp tiles of a pipelined sweep over the box [0,nx)x[0,ny)x[0,nz)
+// starting at grid cell `off`, and the progress base of this launch: the
+// launch uses progress values in (base, base + span]; the counters are only
+// compared against later bases, so they need no reset between launches.
+les_status wave_setup(les_ctx* c, int nx, int ny, int nz, int off, int span, Wave& W, int& base)
+{
+    W.nx = nx;
+    W.ny = ny;
+    W.nz = nz;
+    W.si = c->g.si;
+    W.sj = c->g.sj;
+    W.off = off;
+    W.wj = (ny + WAVE_TJ - 1) / WAVE_TJ;
+    W.wk = (nz + 31) / 32;
+    W.ntiles = W.wj * W.wk;
+    W.steps = nx + 31;
+    if (c->wave_prog_len < W.ntiles) {
+        cudaFree(c->wave_prog);
+        c->wave_prog = nullptr;
+        c->wave_prog_len = 0;
+        les_status st = check_cuda(c, cudaMalloc(&c->wave_prog, sizeof(int) * (size_t)W.ntiles), "cudaMalloc(wave)");
+        if (st) return st;
+        c->wave_prog_len = W.ntiles;
+        c->wave_epoch = 0;
+        st = check_cuda(c, cudaMemsetAsync(c->wave_prog, 0, sizeof(int) * (size_t)W.ntiles, c->stream), "memset");
+        if (st) return st;
+    }
+    if (span < 0 || span > (1 << 29)) return fail(c, LES_BAD_ARG, "wavefront: too many sweeps in one launch");
+    if (c->wave_epoch > (1 << 30) - span) {   // restart the counters well before the int range ends
+        les_status st = check_cuda(c, cudaMemsetAsync(c->wave_prog, 0, sizeof(int) * (size_t)c->wave_prog_len,
+                                                      c->stream), "memset");
+        if (st) return st;
+        c->wave_epoch = 0;
+    }
+    base = c->wave_epoch;
+    c->wave_epoch += span + 1;
+    W.prog = c->wave_prog;
+    W.err = (int*)(c->gsync + 2);
+    return LES_OK;
+}
+
+// Cooperative launch of a pipelined sweep: one warp per block, as many blocks
+// as tiles but no more than can be resident at once (the tiles are handed out
+// in producer-first order, so any resident count finishes).
+les_status wave_launch(les_ctx* c, const void* fn, void** args, const Wave& W, GridSync* gs, int pid)
+{
+    int per_sm = 0;
+    les_status st = check_cuda(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32, 0), "occupancy");
+    if (st) return st;
+    if (per_sm < 1) return fail(c, LES_CUDA_ERROR, "wavefront kernel cannot be resident");
+    const long long cap = (long long)per_sm * c->sms;
+    const int grid = (int)(W.ntiles < cap ? W.ntiles : cap);
+    gs->nblocks = (unsigned)grid;
+    // count and generation only: the error word stays set until the host reads it
+    st = check_cuda(c, cudaMemsetAsync(c->gsync, 0, sizeof(unsigned) * 2, c->stream), "reset barrier");
+    if (st) return st;
+    cudaEvent_t e1 = nullptr;
+    if (pid >= 0 && c->prof_on) prof_begin(c, pid, &e1);
+    st = check_cuda(c, cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(32), args, 0, c->stream),
+                    "cooperative launch");
+    ++c->launches;
+    if (e1) cudaEventRecord(e1, c->stream);
+    return st;
 }
 
 }  // namespace
 
 namespace les {
 
+// LES_TIMEOUT (and the flag cleared) if a wavefront wait gave up since the last check.
+les_status wave_check(les_ctx* c) { return check_barrier(c); }
+
 les_status ic_apply_dev(les_ctx* c, const double* r, double* z, const double* const* Lsrc, int skip_done)
 {
     const double* const* L = Lsrc ? Lsrc : (const double* const*)c->L;
-    Plane P = plane_of(c->g);
+    Wave W;
+    int base = 0;
+    les_status st = wave_setup(c, c->g.nx, c->g.ny, c->g.nz, 0, 2 * (c->g.nx + 32), W, base);
+    if (st) return st;
     const double *Lc = L[0], *Lw = L[4], *Ls = L[2], *Lb = L[6];
-    GridSync gs = grid_sync(c, c->sms);
+    GridSync gs = grid_sync(c, 0);
     const SolverState* stp = c->state;
     int skip = skip_done;
-    void* args[] = {&P, (void*)&Lc, (void*)&Lw, (void*)&Ls, (void*)&Lb, (void*)&r, (void*)&z, &gs, (void*)&stp, &skip};
-    return coop_launch(c, (const void*)k_ic_apply<double>, args, nullptr, PROF_IC);
+    void* args[] = {&W, &base, (void*)&Lc, (void*)&Lw, (void*)&Ls, (void*)&Lb, (void*)&r, (void*)&z, &gs,
+                    (void*)&stp, &skip};
+    return wave_launch(c, (const void*)k_ic_wave<double>, args, W, &gs, PROF_IC);
 }
 
 les_status ic_apply_dev32(les_ctx* c, const float* r, float* z, const float* const* L, SolverState* st)
 {
-    Plane P = plane_of(c->g);
+    Wave W;
+    int base = 0;
+    les_status s2 = wave_setup(c, c->g.nx, c->g.ny, c->g.nz, 0, 2 * (c->g.nx + 32), W, base);
+    if (s2) return s2;
     const float *Lc = L[0], *Lw = L[4], *Ls = L[2], *Lb = L[6];
-    GridSync gs = grid_sync(c, c->sms);
+    GridSync gs = grid_sync(c, 0);
     const SolverState* stp = st;
     int skip = st ? 1 : 0;
-    void* args[] = {&P, (void*)&Lc, (void*)&Lw, (void*)&Ls, (void*)&Lb, (void*)&r, (void*)&z, &gs, (void*)&stp, &skip};
-    return coop_launch(c, (const void*)k_ic_apply<float>, args, nullptr, PROF_IC);
+    void* args[] = {&W, &base, (void*)&Lc, (void*)&Lw, (void*)&Ls, (void*)&Lb, (void*)&r, (void*)&z, &gs,
+                    (void*)&stp, &skip};
+    return wave_launch(c, (const void*)k_ic_wave<float>, args, W, &gs, PROF_IC);
 }
 
 les_status build_ic_dev(les_ctx* c)
@@ -320,9 +673,8 @@ les_status solve_gs_dev(les_ctx* c, double dt, double rho, int max_iter, double 
     const les_mesh& m = c->mesh;
     Plane P = plane_of(c->g);
     double* rhs = c->w[0];
-    // one slot per block of the cooperative grid (partials holds >= 4096)
+    // one slot per warp of the cooperative grid
     double* block_max = c->partials;
-    if ((size_t)c->sms > c->partials_len) return fail(c, LES_BAD_ARG, "internal: partials too small");
     launch(c, k_stat_rhs_gs, (c->g.n + 255) / 256, 256, P, rho / dt, 2 * m.dx, 2 * m.dy, 2 * m.dz,
                                                                c->slot[LES_U], c->slot[LES_V], c->slot[LES_W],
                                                                rhs, c->g.n);
@@ -330,15 +682,27 @@ les_status solve_gs_dev(les_ctx* c, double dt, double rho, int max_iter, double 
     if (st) return st;
     const double dx2 = m.dx * m.dx, dy2 = m.dy * m.dy, dz2 = m.dz * m.dz;
     const double coef = 1.0 / (2.0 * (1.0 / dx2 + 1.0 / dy2 + 1.0 / dz2));
+    const Geo& g = c->g;
+    if (g.nx < 3 || g.ny < 3 || g.nz < 3) return fail(c, LES_BAD_ARG, "GS-SOR needs an interior");
+    Wave W;
+    int base = 0;
+    st = wave_setup(c, g.nx - 2, g.ny - 2, g.nz - 2, g.si + g.sj + 1, max_iter * (g.nx - 2 + 32), W, base);
+    if (st) return st;
+    // x / d2 for a power of two d2 is exactly x * (1 / d2)
+    auto pow2 = [](double v) { int e; return std::frexp(v, &e) == 0.5; };
+    const bool p2 = pow2(dx2) && pow2(dy2) && pow2(dz2);
+    double d2x = p2 ? 1.0 / dx2 : dx2, d2y = p2 ? 1.0 / dy2 : dy2, d2z = p2 ? 1.0 / dz2 : dz2;
     double* p = c->slot[LES_P];
     const uint8_t* solid = c->mask;
     const int* list = c->solid_list;
     int ns = c->n_solid;
     SolverState* stp = c->state;
-    GridSync gs = grid_sync(c, c->sms);
-    void* args[] = {&P, (void*)&dx2, (void*)&dy2, (void*)&dz2, &omega, (void*)&coef, &tol, &max_iter,
-                    (void*)&rhs, &p, (void*)&solid, (void*)&list, &ns, &block_max, &stp, &gs};
-    st = coop_launch(c, (const void*)k_gs_sor, args, nullptr);
+    GridSync gs = grid_sync(c, 0);
+    int nx = g.nx, ny = g.ny, nz = g.nz;
+    void* args[] = {&W, &base, &d2x, &d2y, &d2z, &omega, (void*)&coef, &tol, &max_iter, (void*)&rhs, &p,
+                    (void*)&solid, (void*)&list, &ns, &block_max, &stp, &gs, &nx, &ny, &nz};
+    if ((size_t)W.ntiles > c->partials_len) return fail(c, LES_BAD_ARG, "internal: partials too small");
+    st = wave_launch(c, p2 ? (const void*)k_gs_wave<true> : (const void*)k_gs_wave<false>, args, W, &gs, -1);
     if (st) return st;
     st = check_barrier(c);
     if (st) return st;
