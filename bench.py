@@ -202,11 +202,16 @@ def step_params(G, les_cases, precond, lmax, precision, inner_rtol=1e-4, solver=
         return G.step_params(nu=les_cases.NU, rho=les_cases.RHO, cs=les_cases.CS, cfl_conv=les_cases.CFL_CONV,
                              cfl_visc=les_cases.CFL_VISC, dt_max=les_cases.DT_MAX, solver=G.SOLVER_GS,
                              stat_max_iter=200, stat_tol=1e-6, omega=1.7)
+    # IC(0)-PCG does not converge on this non-symmetric system (the reference's
+    # own run stalls): it runs to the reference's cap of 1000 iterations
+    # (src/main.cpp:137) in both precisions
+    cap = 1000 if precond == "ic" else None
     if precision == G.MIXED:
-        opts = G.pcg_opts(precond=pc, max_iter=50000, lambda_min=3 * np.pi ** 2, lambda_max=lmax, degree=4,
-                          precision=G.MIXED, inner_rtol=inner_rtol, inner_max_iter=5000, max_outer=40)
+        opts = G.pcg_opts(precond=pc, max_iter=cap or 50000, lambda_min=3 * np.pi ** 2, lambda_max=lmax, degree=4,
+                          precision=G.MIXED, inner_rtol=inner_rtol, inner_max_iter=cap or 5000,
+                          max_outer=1 if cap else 40)
     else:
-        opts = G.pcg_opts(precond=pc, max_iter=10000, lambda_min=3 * np.pi ** 2, lambda_max=lmax, degree=4)
+        opts = G.pcg_opts(precond=pc, max_iter=cap or 10000, lambda_min=3 * np.pi ** 2, lambda_max=lmax, degree=4)
     return G.step_params(nu=les_cases.NU, rho=les_cases.RHO, cs=les_cases.CS, cfl_conv=les_cases.CFL_CONV,
                          cfl_visc=les_cases.CFL_VISC, dt_max=les_cases.DT_MAX, solver=G.SOLVER_PCG,
                          rel_tol=1e-8, pcg=opts)
@@ -242,7 +247,8 @@ class OracleCase:
         if solver == "gs":
             self.prm = O.StepParams(solver=2, max_iter=200, tol=1e-6, rel_tol=0.0, **common)
         else:
-            self.prm = O.StepParams(solver=0, max_iter=10000, tol=0.0, rel_tol=1e-8, **common)
+            self.prm = O.StepParams(solver=0, max_iter=1000 if precond == "ic" else 10000, tol=0.0, rel_tol=1e-8,
+                                    **common)
 
     def step(self):
         """One full step; returns (seconds, solver iterations)."""

@@ -172,14 +172,38 @@ __device__ __forceinline__ bool wait_batch(const Wave& W, const TileDeps& d, int
     return ok != 0;
 }
 
+// ---- operand staging: every step's read-only (or not yet written) operands
+// are copied into shared memory WD steps ahead with cp.async, so a step
+// never waits on a global load; only the cross-tile neighbours (after the
+// batch's wait) are read directly.
+constexpr int WD = 8;   // steps staged ahead (a power of two)
+
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* smem, const void* gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(s), "l"(gmem), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 // IC(0) substitution of one tile, src/pressure.cpp:442-482.  DIR > 0: the
 // forward solve L y = r (z = y); DIR < 0: the backward solve L^T z = y.
 // Row r of the tile is grid row j = jb + r (forward) or jb + rows-1-r
 // (backward); lane l is column k = K*32 + l and starts plane i after
-// skew(l) steps (l forward, 31-l backward).
+// skew(l) steps (l forward, 31-l backward).  Staged per step and row: the
+// right-hand side (forward r, backward this cell's forward result, written
+// only by this lane), Lc and the three off-diagonal factors of the row.
+template <typename T>
+struct IcStage {
+    T v[WD][5][WAVE_TJ][32];
+};
+
 template <typename T, int DIR>
 __device__ bool ic_tile(const Wave& W, int t, int base, const T* __restrict__ Lc, const T* __restrict__ Lw,
-                        const T* __restrict__ Ls, const T* __restrict__ Lb, const T* __restrict__ r, T* z)
+                        const T* __restrict__ Ls, const T* __restrict__ Lb, const T* __restrict__ r, T* z,
+                        IcStage<T>& sg)
 {
     constexpr int TJ = WAVE_TJ;
     constexpr unsigned FULL = 0xffffffffu;
@@ -188,78 +212,115 @@ __device__ bool ic_tile(const Wave& W, int t, int base, const T* __restrict__ Lc
     const int jb = J * TJ, rows = min(TJ, W.ny - jb);
     const int k = K * 32 + lane;
     const bool kin = k < W.nz;
+    const int kc = min(k, W.nz - 1);                          // every address stays inside the grid
     const int sk = DIR > 0 ? lane : 31 - lane;
     const TileDeps d = tile_deps<DIR>(W, J, K, t);
-    const int jn = DIR > 0 ? jb - 1 : jb + rows;              // neighbour row of row 0
-    const int kn = DIR > 0 ? K * 32 - 1 : K * 32 + 32;        // neighbour column of the near lane
     const int near = DIR > 0 ? 0 : 31;                        // lane that reads the k-producer
-    auto jrow = [&](int q) { return DIR > 0 ? jb + q : jb + rows - 1 - q; };
+    // the j-neighbour row of row 0 and the k-neighbour column of the near lane,
+    // clamped into the grid (they are used only when they exist)
+    const int jn = DIR > 0 ? max(jb - 1, 0) : min(jb + rows, W.ny - 1);
+    const int kn = DIR > 0 ? max(K * 32 - 1, 0) : min(K * 32 + 32, W.nz - 1);
+    // row s2 -> index of (i = 0, j, kc), its neighbour-in-grid flags and
+    // offsets (rows past the grid repeat the last row; their results are dropped)
+    int rb[TJ], rkn[TJ];
+    bool jin[TJ];
+#pragma unroll
+    for (int s2 = 0; s2 < TJ; ++s2) {
+        const int q = min(s2, rows - 1);
+        const int j = DIR > 0 ? jb + q : jb + rows - 1 - q;
+        rb[s2] = W.off + j * W.sj + kc;
+        rkn[s2] = W.off + j * W.sj + kn;
+        jin[s2] = DIR > 0 ? j > 0 : j < W.ny - 1;
+    }
+    const bool kbn = DIR > 0 ? k > 0 : k < W.nz - 1;
+    const int es = DIR > 0 ? 0 : W.si, ej = DIR > 0 ? 0 : W.sj, ek = DIR > 0 ? 0 : 1;   // backward: L at the neighbour
     auto plane = [&](int tau, int skew) { return DIR > 0 ? tau - skew : W.nx - 1 - (tau - skew); };
+    auto clampi = [&](int i) { return min(max(i, 0), W.nx - 1); };
+    // stage the operands of step tau into slot tau % WD (one commit group per
+    // step); the neighbour factors of a missing neighbour are read from the
+    // cell itself and not used
+    auto stage = [&](int tau) {
+        const int i = clampi(plane(tau, sk));
+        const int sl = tau & (WD - 1);
+        const int ie = DIR > 0 ? 0 : (i < W.nx - 1 ? W.si : 0);
+#pragma unroll
+        for (int s2 = 0; s2 < TJ; ++s2) {
+            const int id = rb[s2] + i * W.si;
+            const int je = DIR > 0 ? 0 : (jin[s2] ? W.sj : 0);
+            const int ke = DIR > 0 ? 0 : (kbn ? 1 : 0);
+            cp_async<sizeof(T)>(&sg.v[sl][0][s2][lane], (DIR > 0 ? r : z) + id);
+            cp_async<sizeof(T)>(&sg.v[sl][1][s2][lane], Lw + id + ie);
+            cp_async<sizeof(T)>(&sg.v[sl][2][s2][lane], Ls + id + je);
+            cp_async<sizeof(T)>(&sg.v[sl][3][s2][lane], Lb + id + ke);
+            cp_async<sizeof(T)>(&sg.v[sl][4][s2][lane], Lc + id);
+        }
+        cp_commit();
+    };
+    (void)es; (void)ej; (void)ek;
     T prev[TJ], outp[TJ];
 #pragma unroll
     for (int q = 0; q < TJ; ++q) prev[q] = outp[q] = T(0);
+#pragma unroll
+    for (int q = 0; q < WD - 1; ++q) stage(q);
     for (int tau0 = 0; tau0 < W.steps; tau0 += WB) {
         const int tend = min(tau0 + WB, W.steps);
-        if (!wait_batch(W, d, base, tend)) return false;
+        if (!wait_batch(W, d, base, tend)) {
+            cp_wait<0>();
+            return false;
+        }
         // the batch's cross-tile neighbours, through L2: the j-neighbour of
         // row 0 for every step (own column), and the k-neighbours of the near
-        // lane (lane q holds those of step tau0 + q)
+        // lane (lane q holds those of step tau0 + q); clamped loads, selected
         T zj[WB], zk0[TJ];
 #pragma unroll
         for (int q = 0; q < WB; ++q) {
             const int i = plane(tau0 + q, sk);
-            zj[q] = (d.dj >= 0 && kin && tau0 + q < tend && i >= 0 && i < W.nx)
-                        ? __ldcg(z + W.off + i * W.si + jn * W.sj + k) : T(0);
+            const T v = __ldcg(z + W.off + clampi(i) * W.si + jn * W.sj + kc);
+            zj[q] = d.dj >= 0 ? v : T(0);
         }
         {
-            const int i = plane(tau0 + lane, 0);
-            const bool ok = d.dk >= 0 && lane < WB && tau0 + lane < tend && i >= 0 && i < W.nx;
+            const int i = clampi(plane(tau0 + (lane & (WB - 1)), 0));
 #pragma unroll
-            for (int q = 0; q < TJ; ++q)
-                zk0[q] = (ok && q < rows) ? __ldcg(z + W.off + i * W.si + jrow(q) * W.sj + kn) : T(0);
+            for (int q = 0; q < TJ; ++q) {
+                const T v = __ldcg(z + rkn[q] + i * W.si);
+                zk0[q] = d.dk >= 0 ? v : T(0);
+            }
         }
 #pragma unroll
         for (int q = 0; q < WB; ++q) {
             const int tau = tau0 + q;
             if (tau >= tend) break;   // warp-uniform
+            stage(tau + WD - 1);      // past the last step: clamped copies, never used
+            cp_wait<WD - 1>();        // step tau's operands are in
             const int i = plane(tau, sk);
             const bool act = kin && i >= 0 && i < W.nx;
-            T zk[TJ];
-#pragma unroll
-            for (int s2 = 0; s2 < TJ; ++s2) {
-                zk[s2] = DIR > 0 ? __shfl_up_sync(FULL, outp[s2], 1) : __shfl_down_sync(FULL, outp[s2], 1);
-                const T v = __shfl_sync(FULL, zk0[s2], q);
-                if (lane == near) zk[s2] = v;
-            }
+            const int ic = clampi(i);
+            const int sl = tau & (WD - 1);
+            const bool ib = DIR > 0 ? i > 0 : i < W.nx - 1;
             T out[TJ];
 #pragma unroll
             for (int s2 = 0; s2 < TJ; ++s2) {
-                out[s2] = T(0);
-                if (act && s2 < rows) {
-                    const int j = jrow(s2);
-                    const int id = W.off + i * W.si + j * W.sj + k;
-                    const T zjv = s2 == 0 ? zj[q] : out[s2 - 1];
-                    T sum;
-                    if (DIR > 0) {   // :451-463
-                        sum = r[id];
-                        if (i > 0) sum -= Lw[id] * prev[s2];
-                        if (j > 0) sum -= Ls[id] * zjv;
-                        if (k > 0) sum -= Lb[id] * zk[s2];
-                    } else {         // :469-481
-                        sum = __ldcg(z + id);
-                        if (i < W.nx - 1) sum -= Lw[id + W.si] * prev[s2];
-                        if (j < W.ny - 1) sum -= Ls[id + W.sj] * zjv;
-                        if (k < W.nz - 1) sum -= Lb[id + 1] * zk[s2];
-                    }
-                    out[s2] = sum / Lc[id];
-                    z[id] = out[s2];
-                }
+                T zk = DIR > 0 ? __shfl_up_sync(FULL, outp[s2], 1) : __shfl_down_sync(FULL, outp[s2], 1);
+                const T v = __shfl_sync(FULL, zk0[s2], q);
+                zk = lane == near ? v : zk;
+                const T zjv = s2 == 0 ? zj[q] : out[s2 - 1];
+                // :451-463 / :469-481, the terms in the reference's order
+                T sum = sg.v[sl][0][s2][lane];
+                T a = sum - sg.v[sl][1][s2][lane] * prev[s2];
+                sum = ib ? a : sum;
+                a = sum - sg.v[sl][2][s2][lane] * zjv;
+                sum = jin[s2] ? a : sum;
+                a = sum - sg.v[sl][3][s2][lane] * zk;
+                sum = kbn ? a : sum;
+                out[s2] = sum / sg.v[sl][4][s2][lane];
+                if (act && s2 < rows) z[rb[s2] + ic * W.si] = out[s2];
             }
 #pragma unroll
             for (int s2 = 0; s2 < TJ; ++s2) prev[s2] = outp[s2] = out[s2];
         }
         publish(W.prog + t, base + tend);
     }
+    cp_wait<0>();
     return true;
 }
 
@@ -274,12 +335,13 @@ __global__ void __launch_bounds__(32) k_ic_wave(Wave W, int base, const T* __res
                                                 int skip_done)
 {
     if (skip_done && st && st->done) return;   // uniform across blocks: no barrier is entered
+    __shared__ IcStage<T> sg;
     const int w = blockIdx.x, nw = gridDim.x;  // one warp per block
     bool ok = true;
-    for (int t = w; t < W.ntiles && ok; t += nw) ok = ic_tile<T, 1>(W, t, base, Lc, Lw, Ls, Lb, r, z);
+    for (int t = w; t < W.ntiles && ok; t += nw) ok = ic_tile<T, 1>(W, t, base, Lc, Lw, Ls, Lb, r, z, sg);
     if (!grid_barrier(gs) || !ok) return;
     for (int t = w; t < W.ntiles && ok; t += nw)
-        ok = ic_tile<T, -1>(W, W.ntiles - 1 - t, base + W.steps + 1, Lc, Lw, Ls, Lb, r, z);
+        ok = ic_tile<T, -1>(W, W.ntiles - 1 - t, base + W.steps + 1, Lc, Lw, Ls, Lb, r, z, sg);
 }
 
 // One lexicographic SOR sweep of one tile over the interior, :216-234:
@@ -287,11 +349,22 @@ __global__ void __launch_bounds__(32) k_ic_wave(Wave W, int base, const T* __res
 // with the west, south and bottom neighbours already updated in this sweep
 // and the east, north and top ones not yet.  POW2: dx2, dy2, dz2 are powers
 // of two, so x / d2 is exactly x * (1 / d2) and the divisions become
-// multiplications (same results bit for bit).  Returns the tile's max |dp| in
-// *res (per lane).
+// multiplications (same results bit for bit).  Accumulates the tile's max
+// |dp| into maxr (per lane).
+// Staged WD steps ahead: the old values a step reads -- its cells, their
+// east, north and top neighbours -- and rhs.  Those cells are written only at
+// later steps: the cell by this lane at its step, the east one a step later,
+// the top one by the next lane a step later, the row above the tile by the
+// tile above, which waits for this tile's progress (published only after the
+// copies it read were complete).
+struct GsStage {
+    double v[WD][4][WAVE_TJ][32];   // p, p_east, p_top, rhs per row
+    double pn[WD][32];              // the row above the tile
+};
+
 template <bool POW2>
 __device__ bool gs_tile(const Wave& W, int t, int base, double d2x, double d2y, double d2z, double one_m_omega,
-                        double omega_coef, const double* __restrict__ rhs, double* p, double& maxr)
+                        double omega_coef, const double* __restrict__ rhs, double* p, double& maxr, GsStage& sg)
 {
     constexpr int TJ = WAVE_TJ;
     constexpr unsigned FULL = 0xffffffffu;
@@ -300,95 +373,92 @@ __device__ bool gs_tile(const Wave& W, int t, int base, double d2x, double d2y, 
     const int jb = J * TJ, rows = min(TJ, W.ny - jb);
     const int k = K * 32 + lane;   // interior coordinates: grid cell (i+1, j+1, k+1)
     const bool kin = k < W.nz;
+    const int kc = min(k, W.nz - 1);
     const TileDeps d = tile_deps<1>(W, J, K, t);
     const int ssi = W.si, ssj = W.sj;
+    // (i = 0, row s2) of this lane; rows past the grid repeat the last row
+    int rb[TJ];
+#pragma unroll
+    for (int s2 = 0; s2 < TJ; ++s2) rb[s2] = W.off + (jb + min(s2, rows - 1)) * ssj + kc;
+    const int rn = W.off + (jb + rows) * ssj + kc;   // the row above the tile (the wall row past the last tile)
+    const int rs = W.off + (jb - 1) * ssj + kc;      // the row below (the wall row before the first tile)
+    auto div2 = [&](double x, double dd) { return POW2 ? x * dd : x / dd; };
+    auto clampi = [&](int i) { return min(max(i, 0), W.nx - 1); };
+    auto stage = [&](int tau) {
+        const int i = clampi(tau - lane);
+        const int sl = tau & (WD - 1);
+#pragma unroll
+        for (int s2 = 0; s2 < TJ; ++s2) {
+            const int id = rb[s2] + i * ssi;
+            cp_async<8>(&sg.v[sl][0][s2][lane], p + id);
+            cp_async<8>(&sg.v[sl][1][s2][lane], p + id + ssi);
+            cp_async<8>(&sg.v[sl][2][s2][lane], p + id + 1);
+            cp_async<8>(&sg.v[sl][3][s2][lane], rhs + id);
+        }
+        cp_async<8>(&sg.pn[sl][lane], p + rn + i * ssi);
+        cp_commit();
+    };
     double prev[TJ], outp[TJ];
 #pragma unroll
     for (int q = 0; q < TJ; ++q) prev[q] = outp[q] = 0.0;
-    auto div2 = [&](double x, double dd) { return POW2 ? x * dd : x / dd; };
-    // Old values a step reads -- its cells and their east, north and top
-    // neighbours, and rhs -- are fetched one step ahead, before the current
-    // step writes: those cells are written only at later steps (the cell by
-    // this lane at its step, the top neighbour by the next lane one step
-    // later, the row above by the tile above, which waits for this one).
-    struct Old {
-        double po[TJ], pe[TJ], pt[TJ], rh[TJ], pw[TJ], pn;
-    };
-    auto fetch = [&](int tau, Old& o) {
-        const int i = tau - lane;
-        const bool act = kin && i >= 0 && i < W.nx;
 #pragma unroll
-        for (int s2 = 0; s2 < TJ; ++s2) {
-            const int id = W.off + i * ssi + (jb + s2) * ssj + k;
-            const bool a = act && s2 < rows;
-            o.po[s2] = a ? __ldcg(p + id) : 0.0;
-            o.pe[s2] = a ? __ldcg(p + id + ssi) : 0.0;
-            o.pt[s2] = a ? __ldcg(p + id + 1) : 0.0;
-            o.rh[s2] = a ? rhs[id] : 0.0;
-            o.pw[s2] = (a && i == 0) ? __ldcg(p + id - ssi) : 0.0;   // plane i = 0: the inlet face
-        }
-        o.pn = act ? __ldcg(p + W.off + i * ssi + (jb + rows) * ssj + k) : 0.0;
-    };
-    Old nx_old;
-    fetch(0, nx_old);
+    for (int q = 0; q < WD - 1; ++q) stage(q);
     for (int tau0 = 0; tau0 < W.steps; tau0 += WB) {
         const int tend = min(tau0 + WB, W.steps);
-        if (!wait_batch(W, d, base, tend)) return false;
+        if (!wait_batch(W, d, base, tend)) {
+            cp_wait<0>();
+            return false;
+        }
         // the row below the tile (updated by the tile below, or the wall row
         // j = 0) for every step, and the column before the near lane's (the
-        // tile before in k, or the wall column k = 0) for the batch
+        // tile before in k, or the wall column k = 0) for the batch: clamped loads
         double ps0[WB], pb0[TJ];
 #pragma unroll
-        for (int q = 0; q < WB; ++q) {
-            const int i = tau0 + q - lane;
-            ps0[q] = (kin && tau0 + q < tend && i >= 0 && i < W.nx)
-                         ? __ldcg(p + W.off + i * ssi + (jb - 1) * ssj + k) : 0.0;
-        }
+        for (int q = 0; q < WB; ++q) ps0[q] = __ldcg(p + rs + clampi(tau0 + q - lane) * ssi);
         {
-            const int i = tau0 + lane;
-            const bool ok = lane < WB && tau0 + lane < tend && i >= 0 && i < W.nx;
+            const int i = clampi(tau0 + (lane & (WB - 1)));
 #pragma unroll
             for (int q = 0; q < TJ; ++q)
-                pb0[q] = (ok && q < rows) ? __ldcg(p + W.off + i * ssi + (jb + q) * ssj + K * 32 - 1) : 0.0;
+                pb0[q] = __ldcg(p + W.off + i * ssi + (jb + min(q, rows - 1)) * ssj + K * 32 - 1);
         }
 #pragma unroll
         for (int q = 0; q < WB; ++q) {
             const int tau = tau0 + q;
             if (tau >= tend) break;   // warp-uniform
+            stage(tau + WD - 1);
+            cp_wait<WD - 1>();        // step tau's old values are in
             const int i = tau - lane;
             const bool act = kin && i >= 0 && i < W.nx;
-            const Old o = nx_old;
-            if (tau + 1 < W.steps) fetch(tau + 1, nx_old);
-            double pb[TJ];
+            const int ic = clampi(i);
+            const int sl = tau & (WD - 1);
+            // plane i = 0: the west neighbour is the inlet face
+            double pw0[TJ];
 #pragma unroll
-            for (int s2 = 0; s2 < TJ; ++s2) {
-                pb[s2] = __shfl_up_sync(FULL, outp[s2], 1);
-                const double v = __shfl_sync(FULL, pb0[s2], q);
-                if (lane == 0) pb[s2] = v;
-            }
+            for (int s2 = 0; s2 < TJ; ++s2) pw0[s2] = i == 0 ? __ldcg(p + rb[s2] - ssi) : prev[s2];
             double out[TJ];
 #pragma unroll
             for (int s2 = 0; s2 < TJ; ++s2) {
-                out[s2] = 0.0;
-                if (act && s2 < rows) {
-                    const int id = W.off + i * ssi + (jb + s2) * ssj + k;
-                    const double pw = i == 0 ? o.pw[s2] : prev[s2];
-                    const double ps = s2 == 0 ? ps0[q] : out[s2 - 1];
-                    const double pn = s2 + 1 < rows ? o.po[s2 + 1] : o.pn;
-                    const double v = one_m_omega * o.po[s2] +
-                                     omega_coef * ((div2(o.pe[s2] + pw, d2x) + div2(pn + ps, d2y)) +
-                                                   div2(o.pt[s2] + pb[s2], d2z) - o.rh[s2]);
-                    p[id] = v;
-                    out[s2] = v;
-                    const double res = fabs(v - o.po[s2]);
-                    if (res > maxr) maxr = res;
-                }
+                double pb = __shfl_up_sync(FULL, outp[s2], 1);
+                const double v0 = __shfl_sync(FULL, pb0[s2], q);
+                pb = lane == 0 ? v0 : pb;
+                const double ps = s2 == 0 ? ps0[q] : out[s2 - 1];
+                const double po = sg.v[sl][0][s2][lane];
+                const double pn = s2 + 1 < rows ? sg.v[sl][0][s2 + 1 < TJ ? s2 + 1 : s2][lane] : sg.pn[sl][lane];
+                const double v = one_m_omega * po +
+                                 omega_coef * ((div2(sg.v[sl][1][s2][lane] + pw0[s2], d2x) + div2(pn + ps, d2y)) +
+                                               div2(sg.v[sl][2][s2][lane] + pb, d2z) - sg.v[sl][3][s2][lane]);
+                out[s2] = v;
+                const bool own = act && s2 < rows;
+                if (own) p[rb[s2] + ic * ssi] = v;
+                const double res = fabs(v - po);
+                maxr = (own && res > maxr) ? res : maxr;
             }
 #pragma unroll
             for (int s2 = 0; s2 < TJ; ++s2) prev[s2] = outp[s2] = out[s2];
         }
         publish(W.prog + t, base + tend);
     }
+    cp_wait<0>();
     return true;
 }
 
@@ -403,6 +473,7 @@ __global__ void __launch_bounds__(32) k_gs_wave(Wave W, int base, double d2x, do
                                                 int n_solid, double* block_max, SolverState* st, GridSync gs,
                                                 int nx, int ny, int nz)
 {
+    __shared__ GsStage sg;
     const int w = blockIdx.x, nw = gridDim.x;   // one warp per block
     const int lane = threadIdx.x & 31;
     const int gt = w * 32 + lane, gn = nw * 32;
@@ -417,7 +488,7 @@ __global__ void __launch_bounds__(32) k_gs_wave(Wave W, int base, double d2x, do
         bool ok = true;
         const int b = base + iter * (W.steps + 1);
         for (int t = w; t < W.ntiles && ok; t += nw)
-            ok = gs_tile<POW2>(W, t, b, d2x, d2y, d2z, one_m_omega, omega_coef, rhs, p, maxr);
+            ok = gs_tile<POW2>(W, t, b, d2x, d2y, d2z, one_m_omega, omega_coef, rhs, p, maxr, sg);
         if (!grid_barrier(gs) || !ok) return;
         // apply_pressure_BCs faces: every face cell from interior values
         {

@@ -103,3 +103,56 @@ def test_tangent_linear_dot_product_test():
         dJ = c.adjoint_tangent(d_in, d_cs)
     proj = float(np.dot(g, d_in) + gcs * d_cs)
     assert abs(dJ - proj) <= 1e-8 * abs(proj), (dJ, proj)
+
+
+def test_adjoint_c4_recipe_16_random_entries_64x32x32():
+    """The C4 validation recipe on a 64x32x32 grid (h = 1/32, the centred
+    obstacle, probe box [48,60)x[8,24)x[8,24), fixed dt from the initial CFL
+    value, every pressure solve to relative residual 1e-12, checkpoints every
+    8 of 24 steps): the gradient at the uniform inlet u = 1 against central
+    finite differences with step 1e-6 on 16 seeded interior inlet entries
+    and on Cs, each within 1e-5 relative."""
+    shape, h = (64, 32, 32), 1.0 / 32
+    n = int(np.prod(shape))
+    solid = les_cases.box_mask(shape, (16, 24, 12, 20, 12, 20))
+    f = les_cases.init_fields(shape, 0.01, 1234)
+    les_cases.velocity_bcs_np(shape, f, solid)
+    box = (48, 60, 8, 24, 8, 24)
+    nsteps, every, tol, hs = 24, 8, 1e-12, 1e-6
+    m = G.Mesh(*shape, h, h, h)
+
+    def run(prof, cs, grad=False):
+        with G.Context(m) as c:
+            c.upload_mask(np.zeros(n, np.uint8))
+            c.build_stencil()
+            lmax = c.lambda_max(20)
+            c.upload_fields(f)
+            c.upload_mask(solid)
+            c.set_inlet(prof)
+            c.velocity_bcs()
+            dt = c.adaptive_dt(les_cases.NU, les_cases.CFL_CONV, les_cases.CFL_VISC, les_cases.DT_MAX)
+            prm = G.step_params(nu=les_cases.NU, rho=les_cases.RHO, cs=cs, dt_fixed=dt, solver=G.SOLVER_PCG,
+                                rel_tol=tol,
+                                pcg=G.pcg_opts(precond=G.PC_CHEBYSHEV, max_iter=50000, lambda_min=3 * np.pi ** 2,
+                                               lambda_max=lmax, degree=4, precision=G.MIXED, inner_rtol=1e-4))
+            J = c.adjoint_forward(prm, nsteps, every, box, tol)
+            return (J,) + c.adjoint_backward() if grad else J
+
+    prof0 = np.ones(shape[1] * shape[2])
+    cs0 = les_cases.CS
+    J, g, gcs = run(prof0, cs0, grad=True)
+    rng = np.random.default_rng(1234)
+    cand = [(j, k) for j in range(1, shape[1] - 1) for k in range(1, shape[2] - 1)]
+    errs = []
+    for q in rng.choice(len(cand), 16, replace=False):
+        j, k = cand[q]
+        idx = j * shape[2] + k
+        p1, p2 = prof0.copy(), prof0.copy()
+        p1[idx] += hs
+        p2[idx] -= hs
+        fd = (run(p1, cs0) - run(p2, cs0)) / (2 * hs)
+        errs.append(abs(fd - g[idx]) / abs(g[idx]))
+    fdc = (run(prof0, cs0 + hs) - run(prof0, cs0 - hs)) / (2 * hs)
+    errs.append(abs(fdc - gcs) / abs(gcs))
+    print("C4 recipe at 64x32x32: max relative error %.2e (Cs %.2e)" % (max(errs), errs[-1]))
+    assert max(errs) < 1e-5, errs
