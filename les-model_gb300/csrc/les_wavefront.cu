@@ -10,19 +10,23 @@
 // lexicographic loop: the results are bit-identical to the reference.
 //
 // The substitution and the SOR sweep run as a pipelined wavefront with no
-// grid barrier inside a sweep.  The (j, k) plane is cut into warp tiles of TJ
-// rows by 32 columns; a warp owns a tile and marches along i.  Lane l works
-// on plane i = tau - l at its step tau (the lanes are skewed by one plane), so
-// the k-1 neighbour of a cell is lane l-1's result of the step before (a warp
-// shuffle), the j-1 neighbour is the row before in the same thread, and the
-// i-1 neighbour is the thread's own result of the step before.  Only a tile's
-// first row and its first lane need values of other tiles: the tile below in
-// j and the tile before in k publish their progress (steps completed, one
-// counter per tile, release store after a fence) every WB steps, and a warp
-// waits (acquire load, bounded by %globaltimer) for the progress its next WB
-// steps need, then reads those neighbours through L2.  The backward solve
-// mirrors every direction.  Tiles are handed out to the resident warps in an
-// order in which each tile's producers come first, so the waits always end.
+// grid barrier inside a sweep.  The (j, k) plane is cut into tiles of TJ rows
+// by 32 columns; a block of TJ warps owns a tile and marches along i, warp w
+// on the tile's row w and lane l on column l, working at block step tau on
+// plane tau - l - w (lanes and warps skewed by one plane each).  So the k-1
+// neighbour of a cell is the previous lane's result of the step before (a
+// warp shuffle), the j-1 neighbour the previous warp's result of the step
+// before (shared memory, one block barrier per step), and the i-1 neighbour
+// the thread's own result of the step before.  The rows of a tile run on the
+// SM's four sub-partitions at once: a single warp would push all of them
+// through one sub-partition's FP64 unit.  Only a tile's first row and first
+// lane need other tiles' values: the tile below in j and the tile before in
+// k publish their progress (steps completed, one counter per tile, release
+// store after a fence) every WB steps, and a block waits (acquire load,
+// bounded by %globaltimer) for the progress its next WB steps need, then
+// reads those neighbours through L2.  The backward solve mirrors every
+// direction.  Tiles are handed out to the resident blocks in an order in
+// which each tile's producers come first, so the waits always end.
 // The IC factorisation (set-up, once) keeps the simpler form: hyperplanes
 // i+j+k = s in order, one grid barrier between them.  Every wait is bounded
 // (about 2 s); a wait that gives up sets an error flag, every warp leaves,
@@ -78,14 +82,24 @@ __global__ void k_ic_build(Plane P, StencilView A, double* Lc, double* Lw, doubl
 }
 
 // ---- pipelined wavefront -----------------------------------------------------
-constexpr int WB = 8;          // steps between progress publications
-constexpr int WAVE_TJ = 4;     // rows per warp tile
+#ifndef LES_WAVE_WB
+#define LES_WAVE_WB 8
+#endif
+#ifndef LES_WAVE_TJ
+#define LES_WAVE_TJ 4
+#endif
+#ifndef LES_WAVE_WD
+#define LES_WAVE_WD 8
+#endif
+constexpr int WB = LES_WAVE_WB;        // steps between progress publications
+constexpr int WAVE_TJ = LES_WAVE_TJ;   // rows per tile = warps per block (one per SM sub-partition)
+constexpr int WT = 32 * WAVE_TJ;
 
 struct Wave {
     int nx, ny, nz, si, sj;    // the swept box (interior for GS-SOR) and the strides
     int off;                   // index of the box's first cell
-    int wj, wk, ntiles;        // warp tiles along j and k
-    int steps;                 // marching steps of a tile: planes + 31
+    int wj, wk, ntiles;        // tiles along j and k
+    int steps;                 // marching steps of a tile: planes + 31 lane skews + TJ-1 row skews
     int* prog;                 // progress counter per tile
     int* err;                  // set by a wait that gives up
 };
@@ -102,8 +116,8 @@ __device__ __forceinline__ void st_release(int* p, int v)
     asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Lane 0: waits until *p has reached target (wrap-safe); false once the wait
-// gave up (~2 s) or another warp raised the error flag.
+// One thread: waits until *p has reached target (wrap-safe); false once the
+// wait gave up (~2 s) or another block raised the error flag.
 __device__ bool wait_progress(const int* p, int target, int* err)
 {
     if (ld_acquire(p) - target >= 0) return true;
@@ -128,12 +142,12 @@ __device__ __forceinline__ double warp_max_all(double v)
     return v;
 }
 
-// Publishes `value` as the tile's progress after every lane's stores.
+// Publishes `value` as the tile's progress after every thread's stores.
 __device__ __forceinline__ void publish(int* p, int value)
 {
     __threadfence();
-    __syncwarp();
-    if ((threadIdx.x & 31) == 0) st_release(p, value);
+    __syncthreads();
+    if (threadIdx.x == 0) st_release(p, value);
 }
 
 // Tile t's producers: DIR > 0 the tiles below in j (t-1) and before in k
@@ -156,27 +170,28 @@ __device__ __forceinline__ TileDeps tile_deps(const Wave& W, int J, int K, int t
     return d;
 }
 
-// Waits for the progress a batch of steps [tau0, tend) needs: the j-producer
-// must have completed those steps, the k-producer 31 more (its far lane
-// reaches a plane 31 steps after its near lane).  Returns false in every lane
-// when a wait gave up.
-__device__ __forceinline__ bool wait_batch(const Wave& W, const TileDeps& d, int base, int tend)
+// Waits for the progress a batch of steps [tau0, tend) needs.  A tile's row
+// next to this one is its row TJ-1 (skewed TJ-1 steps behind its row 0), so
+// the j-producer must be TJ-1 steps ahead; the k-producer's far lane reaches
+// a plane 31 steps after its near lane.  Returns false in every thread when a
+// wait gave up.
+__device__ __forceinline__ bool wait_batch(const Wave& W, const TileDeps& d, int base, int tend, int* flag)
 {
-    int ok = 1;
-    if ((threadIdx.x & 31) == 0) {
-        if (d.dj >= 0 && !wait_progress(W.prog + d.dj, base + tend, W.err)) ok = 0;
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        if (d.dj >= 0 && !wait_progress(W.prog + d.dj, base + min(tend + WAVE_TJ - 1, W.steps), W.err)) ok = 0;
         if (ok && d.dk >= 0 && !wait_progress(W.prog + d.dk, base + min(tend + 31, W.steps), W.err)) ok = 0;
+        *flag = ok;
     }
-    ok = __shfl_sync(0xffffffffu, ok, 0);
-    __syncwarp();
-    return ok != 0;
+    __syncthreads();
+    return *flag != 0;
 }
 
 // ---- operand staging: every step's read-only (or not yet written) operands
 // are copied into shared memory WD steps ahead with cp.async, so a step
 // never waits on a global load; only the cross-tile neighbours (after the
 // batch's wait) are read directly.
-constexpr int WD = 8;   // steps staged ahead (a power of two)
+constexpr int WD = LES_WAVE_WD;   // steps staged ahead (a power of two)
 
 template <int BYTES>
 __device__ __forceinline__ void cp_async(void* smem, const void* gmem)
@@ -188,135 +203,118 @@ __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_grou
 template <int N>
 __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
-// IC(0) substitution of one tile, src/pressure.cpp:442-482.  DIR > 0: the
-// forward solve L y = r (z = y); DIR < 0: the backward solve L^T z = y.
-// Row r of the tile is grid row j = jb + r (forward) or jb + rows-1-r
-// (backward); lane l is column k = K*32 + l and starts plane i after
-// skew(l) steps (l forward, 31-l backward).  Staged per step and row: the
-// right-hand side (forward r, backward this cell's forward result, written
-// only by this lane), Lc and the three off-diagonal factors of the row.
+// A tile: rows jb.. of TJ rows (the last tile in j may have fewer) by the 32
+// columns K*32..; warp w works on the tile's row w (in the sweep's order) and
+// lane l on column K*32 + l.  At block step tau, warp w lane l works on plane
+// tau - skew(l) - w (forward planes ascend, backward descend; skew(l) is l
+// forward, 31-l backward), so:
+//   the i-neighbour is the thread's own result of the step before,
+//   the k-neighbour the previous lane's result of the step before (shuffle),
+//   the j-neighbour the previous warp's result of the step before, handed
+//   over in shared memory (double-buffered by step parity, one block barrier
+//   per step); row 0 takes it from the tile before in j.
 template <typename T>
 struct IcStage {
-    T v[WD][5][WAVE_TJ][32];
+    T v[WD][5][WAVE_TJ][32];   // rhs (forward r, backward the cell's forward result), Lw, Ls, Lb, Lc
+    T xs[2][WAVE_TJ][32];      // each row's result of the last two steps
+    int flag;
 };
 
+// IC(0) substitution of one tile, src/pressure.cpp:442-482.  DIR > 0: the
+// forward solve L y = r (z = y); DIR < 0: the backward solve L^T z = y.
 template <typename T, int DIR>
 __device__ bool ic_tile(const Wave& W, int t, int base, const T* __restrict__ Lc, const T* __restrict__ Lw,
                         const T* __restrict__ Ls, const T* __restrict__ Lb, const T* __restrict__ r, T* z,
                         IcStage<T>& sg)
 {
-    constexpr int TJ = WAVE_TJ;
     constexpr unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int J = t % W.wj, K = t / W.wj;
-    const int jb = J * TJ, rows = min(TJ, W.ny - jb);
+    const int jb = J * WAVE_TJ, rows = min(WAVE_TJ, W.ny - jb);
     const int k = K * 32 + lane;
     const bool kin = k < W.nz;
     const int kc = min(k, W.nz - 1);                          // every address stays inside the grid
     const int sk = DIR > 0 ? lane : 31 - lane;
     const TileDeps d = tile_deps<DIR>(W, J, K, t);
-    const int near = DIR > 0 ? 0 : 31;                        // lane that reads the k-producer
-    // the j-neighbour row of row 0 and the k-neighbour column of the near lane,
-    // clamped into the grid (they are used only when they exist)
+    const bool wact = w < rows;                               // this warp's row exists
+    // this warp's grid row (rows past the grid repeat the last one; dropped)
+    const int jr = DIR > 0 ? jb + min(w, rows - 1) : jb + rows - 1 - min(w, rows - 1);
+    const int rb = W.off + jr * W.sj + kc;
+    const bool jin = DIR > 0 ? jr > 0 : jr < W.ny - 1;        // the row has its j-neighbour
+    const bool kbn = DIR > 0 ? k > 0 : k < W.nz - 1;
+    // row 0's neighbour row in the tile before, the near lane's neighbour column
     const int jn = DIR > 0 ? max(jb - 1, 0) : min(jb + rows, W.ny - 1);
     const int kn = DIR > 0 ? max(K * 32 - 1, 0) : min(K * 32 + 32, W.nz - 1);
-    // row s2 -> index of (i = 0, j, kc), its neighbour-in-grid flags and
-    // offsets (rows past the grid repeat the last row; their results are dropped)
-    int rb[TJ], rkn[TJ];
-    bool jin[TJ];
-#pragma unroll
-    for (int s2 = 0; s2 < TJ; ++s2) {
-        const int q = min(s2, rows - 1);
-        const int j = DIR > 0 ? jb + q : jb + rows - 1 - q;
-        rb[s2] = W.off + j * W.sj + kc;
-        rkn[s2] = W.off + j * W.sj + kn;
-        jin[s2] = DIR > 0 ? j > 0 : j < W.ny - 1;
-    }
-    const bool kbn = DIR > 0 ? k > 0 : k < W.nz - 1;
-    const int es = DIR > 0 ? 0 : W.si, ej = DIR > 0 ? 0 : W.sj, ek = DIR > 0 ? 0 : 1;   // backward: L at the neighbour
-    auto plane = [&](int tau, int skew) { return DIR > 0 ? tau - skew : W.nx - 1 - (tau - skew); };
+    const int near = DIR > 0 ? 0 : 31;
+    auto plane = [&](int tau, int skew) { return DIR > 0 ? tau - skew - w : W.nx - 1 - (tau - skew - w); };
     auto clampi = [&](int i) { return min(max(i, 0), W.nx - 1); };
-    // stage the operands of step tau into slot tau % WD (one commit group per
-    // step); the neighbour factors of a missing neighbour are read from the
-    // cell itself and not used
+    // the operands of step tau into slot tau % WD (one commit group per step);
+    // the factors of a missing neighbour are read from the cell and not used
     auto stage = [&](int tau) {
         const int i = clampi(plane(tau, sk));
         const int sl = tau & (WD - 1);
+        const int id = rb + i * W.si;
         const int ie = DIR > 0 ? 0 : (i < W.nx - 1 ? W.si : 0);
-#pragma unroll
-        for (int s2 = 0; s2 < TJ; ++s2) {
-            const int id = rb[s2] + i * W.si;
-            const int je = DIR > 0 ? 0 : (jin[s2] ? W.sj : 0);
-            const int ke = DIR > 0 ? 0 : (kbn ? 1 : 0);
-            cp_async<sizeof(T)>(&sg.v[sl][0][s2][lane], (DIR > 0 ? r : z) + id);
-            cp_async<sizeof(T)>(&sg.v[sl][1][s2][lane], Lw + id + ie);
-            cp_async<sizeof(T)>(&sg.v[sl][2][s2][lane], Ls + id + je);
-            cp_async<sizeof(T)>(&sg.v[sl][3][s2][lane], Lb + id + ke);
-            cp_async<sizeof(T)>(&sg.v[sl][4][s2][lane], Lc + id);
-        }
+        const int je = DIR > 0 ? 0 : (jin ? W.sj : 0);
+        const int ke = DIR > 0 ? 0 : (kbn ? 1 : 0);
+        cp_async<sizeof(T)>(&sg.v[sl][0][w][lane], (DIR > 0 ? r : z) + id);
+        cp_async<sizeof(T)>(&sg.v[sl][1][w][lane], Lw + id + ie);
+        cp_async<sizeof(T)>(&sg.v[sl][2][w][lane], Ls + id + je);
+        cp_async<sizeof(T)>(&sg.v[sl][3][w][lane], Lb + id + ke);
+        cp_async<sizeof(T)>(&sg.v[sl][4][w][lane], Lc + id);
         cp_commit();
     };
-    (void)es; (void)ej; (void)ek;
-    T prev[TJ], outp[TJ];
-#pragma unroll
-    for (int q = 0; q < TJ; ++q) prev[q] = outp[q] = T(0);
+    T prev = T(0), outp = T(0);
+    sg.xs[0][w][lane] = sg.xs[1][w][lane] = T(0);
 #pragma unroll
     for (int q = 0; q < WD - 1; ++q) stage(q);
     for (int tau0 = 0; tau0 < W.steps; tau0 += WB) {
         const int tend = min(tau0 + WB, W.steps);
-        if (!wait_batch(W, d, base, tend)) {
+        if (!wait_batch(W, d, base, tend, &sg.flag)) {
             cp_wait<0>();
             return false;
         }
-        // the batch's cross-tile neighbours, through L2: the j-neighbour of
-        // row 0 for every step (own column), and the k-neighbours of the near
-        // lane (lane q holds those of step tau0 + q); clamped loads, selected
-        T zj[WB], zk0[TJ];
+        // the batch's cross-tile neighbours through L2 (clamped loads,
+        // selected): row 0's j-neighbour for every step (own column), and the
+        // k-neighbours of this warp's near lane (lane q holds step tau0 + q's)
+        T zj[WB];
 #pragma unroll
         for (int q = 0; q < WB; ++q) {
-            const int i = plane(tau0 + q, sk);
-            const T v = __ldcg(z + W.off + clampi(i) * W.si + jn * W.sj + kc);
+            const T v = __ldcg(z + W.off + clampi(plane(tau0 + q, sk)) * W.si + jn * W.sj + kc);
             zj[q] = d.dj >= 0 ? v : T(0);
         }
+        T zk0;
         {
-            const int i = clampi(plane(tau0 + (lane & (WB - 1)), 0));
-#pragma unroll
-            for (int q = 0; q < TJ; ++q) {
-                const T v = __ldcg(z + rkn[q] + i * W.si);
-                zk0[q] = d.dk >= 0 ? v : T(0);
-            }
+            const T v = __ldcg(z + W.off + clampi(plane(tau0 + (lane & (WB - 1)), 0)) * W.si + jr * W.sj + kn);
+            zk0 = d.dk >= 0 ? v : T(0);
         }
 #pragma unroll
         for (int q = 0; q < WB; ++q) {
             const int tau = tau0 + q;
-            if (tau >= tend) break;   // warp-uniform
+            if (tau >= tend) break;   // block-uniform
             stage(tau + WD - 1);      // past the last step: clamped copies, never used
             cp_wait<WD - 1>();        // step tau's operands are in
             const int i = plane(tau, sk);
-            const bool act = kin && i >= 0 && i < W.nx;
-            const int ic = clampi(i);
+            const bool act = wact && kin && i >= 0 && i < W.nx;
             const int sl = tau & (WD - 1);
             const bool ib = DIR > 0 ? i > 0 : i < W.nx - 1;
-            T out[TJ];
-#pragma unroll
-            for (int s2 = 0; s2 < TJ; ++s2) {
-                T zk = DIR > 0 ? __shfl_up_sync(FULL, outp[s2], 1) : __shfl_down_sync(FULL, outp[s2], 1);
-                const T v = __shfl_sync(FULL, zk0[s2], q);
-                zk = lane == near ? v : zk;
-                const T zjv = s2 == 0 ? zj[q] : out[s2 - 1];
-                // :451-463 / :469-481, the terms in the reference's order
-                T sum = sg.v[sl][0][s2][lane];
-                T a = sum - sg.v[sl][1][s2][lane] * prev[s2];
-                sum = ib ? a : sum;
-                a = sum - sg.v[sl][2][s2][lane] * zjv;
-                sum = jin[s2] ? a : sum;
-                a = sum - sg.v[sl][3][s2][lane] * zk;
-                sum = kbn ? a : sum;
-                out[s2] = sum / sg.v[sl][4][s2][lane];
-                if (act && s2 < rows) z[rb[s2] + ic * W.si] = out[s2];
-            }
-#pragma unroll
-            for (int s2 = 0; s2 < TJ; ++s2) prev[s2] = outp[s2] = out[s2];
+            T zk = DIR > 0 ? __shfl_up_sync(FULL, outp, 1) : __shfl_down_sync(FULL, outp, 1);
+            const T v0 = __shfl_sync(FULL, zk0, q);
+            zk = lane == near ? v0 : zk;
+            const T zjv = w == 0 ? zj[q] : sg.xs[(tau - 1) & 1][w - 1][lane];
+            // :451-463 / :469-481, the terms in the reference's order
+            T sum = sg.v[sl][0][w][lane];
+            T a = sum - sg.v[sl][1][w][lane] * prev;
+            sum = ib ? a : sum;
+            a = sum - sg.v[sl][2][w][lane] * zjv;
+            sum = jin ? a : sum;
+            a = sum - sg.v[sl][3][w][lane] * zk;
+            sum = kbn ? a : sum;
+            const T out = sum / sg.v[sl][4][w][lane];
+            if (act) z[rb + i * W.si] = out;
+            prev = outp = out;
+            sg.xs[tau & 1][w][lane] = out;
+            __syncthreads();          // the next step reads this step's rows
         }
         publish(W.prog + t, base + tend);
     }
@@ -329,18 +327,18 @@ __device__ bool ic_tile(const Wave& W, int t, int base, const T* __restrict__ Lc
 // reference's arithmetic; T = float serves the FP32 inner solve of the
 // mixed-precision path (st == nullptr: never skipped).
 template <typename T>
-__global__ void __launch_bounds__(32) k_ic_wave(Wave W, int base, const T* __restrict__ Lc, const T* __restrict__ Lw,
+__global__ void __launch_bounds__(WT) k_ic_wave(Wave W, int base, const T* __restrict__ Lc, const T* __restrict__ Lw,
                                                 const T* __restrict__ Ls, const T* __restrict__ Lb,
                                                 const T* __restrict__ r, T* z, GridSync gs, const SolverState* st,
                                                 int skip_done)
 {
     if (skip_done && st && st->done) return;   // uniform across blocks: no barrier is entered
     __shared__ IcStage<T> sg;
-    const int w = blockIdx.x, nw = gridDim.x;  // one warp per block
+    const int b = blockIdx.x, nb = gridDim.x;  // one tile per block at a time
     bool ok = true;
-    for (int t = w; t < W.ntiles && ok; t += nw) ok = ic_tile<T, 1>(W, t, base, Lc, Lw, Ls, Lb, r, z, sg);
+    for (int t = b; t < W.ntiles && ok; t += nb) ok = ic_tile<T, 1>(W, t, base, Lc, Lw, Ls, Lb, r, z, sg);
     if (!grid_barrier(gs) || !ok) return;
-    for (int t = w; t < W.ntiles && ok; t += nw)
+    for (int t = b; t < W.ntiles && ok; t += nb)
         ok = ic_tile<T, -1>(W, W.ntiles - 1 - t, base + W.steps + 1, Lc, Lw, Ls, Lb, r, z, sg);
 }
 
@@ -349,112 +347,89 @@ __global__ void __launch_bounds__(32) k_ic_wave(Wave W, int base, const T* __res
 // with the west, south and bottom neighbours already updated in this sweep
 // and the east, north and top ones not yet.  POW2: dx2, dy2, dz2 are powers
 // of two, so x / d2 is exactly x * (1 / d2) and the divisions become
-// multiplications (same results bit for bit).  Accumulates the tile's max
-// |dp| into maxr (per lane).
-// Staged WD steps ahead: the old values a step reads -- its cells, their
-// east, north and top neighbours -- and rhs.  Those cells are written only at
-// later steps: the cell by this lane at its step, the east one a step later,
-// the top one by the next lane a step later, the row above the tile by the
-// tile above, which waits for this tile's progress (published only after the
-// copies it read were complete).
+// multiplications (same results bit for bit).  Accumulates the thread's max
+// |dp| into maxr.  Staged WD steps ahead: the old values a step reads -- the
+// cell, its east, north and top neighbours -- and rhs.  Those cells are
+// written only at later steps: the cell by this thread at its step, the east
+// one a step later, the north one by the next warp a step later (or by the
+// tile above, which waits for this tile's progress, published only after the
+// copies that read it completed), the top one by the next lane a step later.
 struct GsStage {
-    double v[WD][4][WAVE_TJ][32];   // p, p_east, p_top, rhs per row
-    double pn[WD][32];              // the row above the tile
+    double v[WD][5][WAVE_TJ][32];   // p, p_east, p_north, p_top, rhs
+    double xs[2][WAVE_TJ][32];      // each row's result of the last two steps
+    int flag;
 };
 
 template <bool POW2>
 __device__ bool gs_tile(const Wave& W, int t, int base, double d2x, double d2y, double d2z, double one_m_omega,
                         double omega_coef, const double* __restrict__ rhs, double* p, double& maxr, GsStage& sg)
 {
-    constexpr int TJ = WAVE_TJ;
     constexpr unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int J = t % W.wj, K = t / W.wj;
-    const int jb = J * TJ, rows = min(TJ, W.ny - jb);
+    const int jb = J * WAVE_TJ, rows = min(WAVE_TJ, W.ny - jb);
     const int k = K * 32 + lane;   // interior coordinates: grid cell (i+1, j+1, k+1)
     const bool kin = k < W.nz;
     const int kc = min(k, W.nz - 1);
     const TileDeps d = tile_deps<1>(W, J, K, t);
+    const bool wact = w < rows;
     const int ssi = W.si, ssj = W.sj;
-    // (i = 0, row s2) of this lane; rows past the grid repeat the last row
-    int rb[TJ];
-#pragma unroll
-    for (int s2 = 0; s2 < TJ; ++s2) rb[s2] = W.off + (jb + min(s2, rows - 1)) * ssj + kc;
-    const int rn = W.off + (jb + rows) * ssj + kc;   // the row above the tile (the wall row past the last tile)
-    const int rs = W.off + (jb - 1) * ssj + kc;      // the row below (the wall row before the first tile)
+    const int rb = W.off + (jb + min(w, rows - 1)) * ssj + kc;   // (i = 0, this warp's row)
+    const int rs = W.off + (jb - 1) * ssj + kc;                  // the row below the tile (the wall before the first)
     auto div2 = [&](double x, double dd) { return POW2 ? x * dd : x / dd; };
     auto clampi = [&](int i) { return min(max(i, 0), W.nx - 1); };
     auto stage = [&](int tau) {
-        const int i = clampi(tau - lane);
+        const int id = rb + clampi(tau - lane - w) * ssi;
         const int sl = tau & (WD - 1);
-#pragma unroll
-        for (int s2 = 0; s2 < TJ; ++s2) {
-            const int id = rb[s2] + i * ssi;
-            cp_async<8>(&sg.v[sl][0][s2][lane], p + id);
-            cp_async<8>(&sg.v[sl][1][s2][lane], p + id + ssi);
-            cp_async<8>(&sg.v[sl][2][s2][lane], p + id + 1);
-            cp_async<8>(&sg.v[sl][3][s2][lane], rhs + id);
-        }
-        cp_async<8>(&sg.pn[sl][lane], p + rn + i * ssi);
+        cp_async<8>(&sg.v[sl][0][w][lane], p + id);
+        cp_async<8>(&sg.v[sl][1][w][lane], p + id + ssi);
+        cp_async<8>(&sg.v[sl][2][w][lane], p + id + ssj);   // the row above (the wall past the last row)
+        cp_async<8>(&sg.v[sl][3][w][lane], p + id + 1);
+        cp_async<8>(&sg.v[sl][4][w][lane], rhs + id);
         cp_commit();
     };
-    double prev[TJ], outp[TJ];
-#pragma unroll
-    for (int q = 0; q < TJ; ++q) prev[q] = outp[q] = 0.0;
+    double prev = 0.0, outp = 0.0;
+    sg.xs[0][w][lane] = sg.xs[1][w][lane] = 0.0;
 #pragma unroll
     for (int q = 0; q < WD - 1; ++q) stage(q);
     for (int tau0 = 0; tau0 < W.steps; tau0 += WB) {
         const int tend = min(tau0 + WB, W.steps);
-        if (!wait_batch(W, d, base, tend)) {
+        if (!wait_batch(W, d, base, tend, &sg.flag)) {
             cp_wait<0>();
             return false;
         }
         // the row below the tile (updated by the tile below, or the wall row
-        // j = 0) for every step, and the column before the near lane's (the
-        // tile before in k, or the wall column k = 0) for the batch: clamped loads
-        double ps0[WB], pb0[TJ];
+        // j = 0) for every step of warp 0, and the column before the near
+        // lane's (the tile before in k, or the wall column k = 0): clamped loads
+        double ps0[WB];
 #pragma unroll
         for (int q = 0; q < WB; ++q) ps0[q] = __ldcg(p + rs + clampi(tau0 + q - lane) * ssi);
-        {
-            const int i = clampi(tau0 + (lane & (WB - 1)));
-#pragma unroll
-            for (int q = 0; q < TJ; ++q)
-                pb0[q] = __ldcg(p + W.off + i * ssi + (jb + min(q, rows - 1)) * ssj + K * 32 - 1);
-        }
+        const double pb0 = __ldcg(p + rb - kc + K * 32 - 1 + clampi(tau0 + (lane & (WB - 1)) - w) * ssi);
 #pragma unroll
         for (int q = 0; q < WB; ++q) {
             const int tau = tau0 + q;
-            if (tau >= tend) break;   // warp-uniform
+            if (tau >= tend) break;   // block-uniform
             stage(tau + WD - 1);
             cp_wait<WD - 1>();        // step tau's old values are in
-            const int i = tau - lane;
-            const bool act = kin && i >= 0 && i < W.nx;
-            const int ic = clampi(i);
+            const int i = tau - lane - w;
+            const bool act = wact && kin && i >= 0 && i < W.nx;
             const int sl = tau & (WD - 1);
             // plane i = 0: the west neighbour is the inlet face
-            double pw0[TJ];
-#pragma unroll
-            for (int s2 = 0; s2 < TJ; ++s2) pw0[s2] = i == 0 ? __ldcg(p + rb[s2] - ssi) : prev[s2];
-            double out[TJ];
-#pragma unroll
-            for (int s2 = 0; s2 < TJ; ++s2) {
-                double pb = __shfl_up_sync(FULL, outp[s2], 1);
-                const double v0 = __shfl_sync(FULL, pb0[s2], q);
-                pb = lane == 0 ? v0 : pb;
-                const double ps = s2 == 0 ? ps0[q] : out[s2 - 1];
-                const double po = sg.v[sl][0][s2][lane];
-                const double pn = s2 + 1 < rows ? sg.v[sl][0][s2 + 1 < TJ ? s2 + 1 : s2][lane] : sg.pn[sl][lane];
-                const double v = one_m_omega * po +
-                                 omega_coef * ((div2(sg.v[sl][1][s2][lane] + pw0[s2], d2x) + div2(pn + ps, d2y)) +
-                                               div2(sg.v[sl][2][s2][lane] + pb, d2z) - sg.v[sl][3][s2][lane]);
-                out[s2] = v;
-                const bool own = act && s2 < rows;
-                if (own) p[rb[s2] + ic * ssi] = v;
-                const double res = fabs(v - po);
-                maxr = (own && res > maxr) ? res : maxr;
-            }
-#pragma unroll
-            for (int s2 = 0; s2 < TJ; ++s2) prev[s2] = outp[s2] = out[s2];
+            const double pw = i == 0 ? __ldcg(p + rb - ssi) : prev;
+            double pb = __shfl_up_sync(FULL, outp, 1);
+            const double v0 = __shfl_sync(FULL, pb0, q);
+            pb = lane == 0 ? v0 : pb;
+            const double ps = w == 0 ? ps0[q] : sg.xs[(tau - 1) & 1][w - 1][lane];
+            const double po = sg.v[sl][0][w][lane];
+            const double v = one_m_omega * po +
+                             omega_coef * ((div2(sg.v[sl][1][w][lane] + pw, d2x) + div2(sg.v[sl][2][w][lane] + ps, d2y)) +
+                                           div2(sg.v[sl][3][w][lane] + pb, d2z) - sg.v[sl][4][w][lane]);
+            if (act) p[rb + i * ssi] = v;
+            const double res = fabs(v - po);
+            maxr = (act && res > maxr) ? res : maxr;
+            prev = outp = v;
+            sg.xs[tau & 1][w][lane] = v;
+            __syncthreads();          // the next step reads this step's rows
         }
         publish(W.prog + t, base + tend);
     }
@@ -466,7 +441,7 @@ __device__ bool gs_tile(const Wave& W, int t, int base, double d2x, double d2y, 
 // the interior, each a pipelined wavefront followed by apply_pressure_BCs
 // (face closed form, then the obstacle copy) and the max|dp| < tol test.
 template <bool POW2>
-__global__ void __launch_bounds__(32) k_gs_wave(Wave W, int base, double d2x, double d2y, double d2z, double omega,
+__global__ void __launch_bounds__(WT) k_gs_wave(Wave W, int base, double d2x, double d2y, double d2z, double omega,
                                                 double coef, double tol, int max_iter,
                                                 const double* __restrict__ rhs, double* p,
                                                 const uint8_t* __restrict__ solid, const int* __restrict__ solid_list,
@@ -474,9 +449,10 @@ __global__ void __launch_bounds__(32) k_gs_wave(Wave W, int base, double d2x, do
                                                 int nx, int ny, int nz)
 {
     __shared__ GsStage sg;
-    const int w = blockIdx.x, nw = gridDim.x;   // one warp per block
-    const int lane = threadIdx.x & 31;
-    const int gt = w * 32 + lane, gn = nw * 32;
+    __shared__ double wmax[WAVE_TJ];
+    const int b = blockIdx.x, nb = gridDim.x;   // one tile per block at a time
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int gt = b * WT + threadIdx.x, gn = nb * WT;
     const double one_m_omega = 1 - omega;
     const double omega_coef = omega * coef;
     const int si = ny * nz, sj = nz;
@@ -486,9 +462,9 @@ __global__ void __launch_bounds__(32) k_gs_wave(Wave W, int base, double d2x, do
     for (int iter = 0; iter < max_iter; ++iter) {
         double maxr = 0.0;
         bool ok = true;
-        const int b = base + iter * (W.steps + 1);
-        for (int t = w; t < W.ntiles && ok; t += nw)
-            ok = gs_tile<POW2>(W, t, b, d2x, d2y, d2z, one_m_omega, omega_coef, rhs, p, maxr, sg);
+        const int bs = base + iter * (W.steps + 1);
+        for (int t = b; t < W.ntiles && ok; t += nb)
+            ok = gs_tile<POW2>(W, t, bs, d2x, d2y, d2z, one_m_omega, omega_coef, rhs, p, maxr, sg);
         if (!grid_barrier(gs) || !ok) return;
         // apply_pressure_BCs faces: every face cell from interior values
         {
@@ -530,13 +506,19 @@ __global__ void __launch_bounds__(32) k_gs_wave(Wave W, int base, double d2x, do
             else if (!solid[id + 1]) p[id] = __ldcg(p + id + 1);
             else if (!solid[id - 1]) p[id] = __ldcg(p + id - 1);
         }
-        // warp max -> global max (exact), identical in every lane of every
-        // warp (a butterfly, so that the break below is uniform)
+        // block max -> global max (exact), the same value in every thread (so
+        // that the break below is uniform)
         maxr = warp_max_all(maxr);
-        if (lane == 0) block_max[w] = maxr;
+        if (lane == 0) wmax[w] = maxr;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double m = 0.0;
+            for (int q = 0; q < WAVE_TJ; ++q) m = fmax(m, wmax[q]);
+            block_max[b] = m;
+        }
         if (!grid_barrier(gs)) return;
         double gmax = 0.0;
-        for (int q = lane; q < nw; q += 32) gmax = fmax(gmax, __ldcg(block_max + q));
+        for (int q = lane; q < nb; q += 32) gmax = fmax(gmax, __ldcg(block_max + q));
         gmax = warp_max_all(gmax);
         sweeps = iter + 1;
         if (gmax < tol) { converged = true; break; }
@@ -626,7 +608,7 @@ les_status wave_setup(les_ctx* c, int nx, int ny, int nz, int off, int span, Wav
     W.wj = (ny + WAVE_TJ - 1) / WAVE_TJ;
     W.wk = (nz + 31) / 32;
     W.ntiles = W.wj * W.wk;
-    W.steps = nx + 31;
+    W.steps = nx + 31 + WAVE_TJ - 1;
     if (c->wave_prog_len < W.ntiles) {
         cudaFree(c->wave_prog);
         c->wave_prog = nullptr;
@@ -652,13 +634,13 @@ les_status wave_setup(les_ctx* c, int nx, int ny, int nz, int off, int span, Wav
     return LES_OK;
 }
 
-// Cooperative launch of a pipelined sweep: one warp per block, as many blocks
+// Cooperative launch of a pipelined sweep: one tile per block at a time, as many blocks
 // as tiles but no more than can be resident at once (the tiles are handed out
 // in producer-first order, so any resident count finishes).
 les_status wave_launch(les_ctx* c, const void* fn, void** args, const Wave& W, GridSync* gs, int pid)
 {
     int per_sm = 0;
-    les_status st = check_cuda(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32, 0), "occupancy");
+    les_status st = check_cuda(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, WT, 0), "occupancy");
     if (st) return st;
     if (per_sm < 1) return fail(c, LES_CUDA_ERROR, "wavefront kernel cannot be resident");
     const long long cap = (long long)per_sm * c->sms;
@@ -669,7 +651,7 @@ les_status wave_launch(les_ctx* c, const void* fn, void** args, const Wave& W, G
     if (st) return st;
     cudaEvent_t e1 = nullptr;
     if (pid >= 0 && c->prof_on) prof_begin(c, pid, &e1);
-    st = check_cuda(c, cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(32), args, 0, c->stream),
+    st = check_cuda(c, cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(WT), args, 0, c->stream),
                     "cooperative launch");
     ++c->launches;
     if (e1) cudaEventRecord(e1, c->stream);
@@ -688,7 +670,7 @@ les_status ic_apply_dev(les_ctx* c, const double* r, double* z, const double* co
     const double* const* L = Lsrc ? Lsrc : (const double* const*)c->L;
     Wave W;
     int base = 0;
-    les_status st = wave_setup(c, c->g.nx, c->g.ny, c->g.nz, 0, 2 * (c->g.nx + 32), W, base);
+    les_status st = wave_setup(c, c->g.nx, c->g.ny, c->g.nz, 0, 2 * (c->g.nx + 32 + WAVE_TJ), W, base);
     if (st) return st;
     const double *Lc = L[0], *Lw = L[4], *Ls = L[2], *Lb = L[6];
     GridSync gs = grid_sync(c, 0);
@@ -703,7 +685,7 @@ les_status ic_apply_dev32(les_ctx* c, const float* r, float* z, const float* con
 {
     Wave W;
     int base = 0;
-    les_status s2 = wave_setup(c, c->g.nx, c->g.ny, c->g.nz, 0, 2 * (c->g.nx + 32), W, base);
+    les_status s2 = wave_setup(c, c->g.nx, c->g.ny, c->g.nz, 0, 2 * (c->g.nx + 32 + WAVE_TJ), W, base);
     if (s2) return s2;
     const float *Lc = L[0], *Lw = L[4], *Ls = L[2], *Lb = L[6];
     GridSync gs = grid_sync(c, 0);
@@ -757,7 +739,7 @@ les_status solve_gs_dev(les_ctx* c, double dt, double rho, int max_iter, double 
     if (g.nx < 3 || g.ny < 3 || g.nz < 3) return fail(c, LES_BAD_ARG, "GS-SOR needs an interior");
     Wave W;
     int base = 0;
-    st = wave_setup(c, g.nx - 2, g.ny - 2, g.nz - 2, g.si + g.sj + 1, max_iter * (g.nx - 2 + 32), W, base);
+    st = wave_setup(c, g.nx - 2, g.ny - 2, g.nz - 2, g.si + g.sj + 1, max_iter * (g.nx - 2 + 32 + WAVE_TJ), W, base);
     if (st) return st;
     // x / d2 for a power of two d2 is exactly x * (1 / d2)
     auto pow2 = [](double v) { int e; return std::frexp(v, &e) == 0.5; };
