@@ -468,18 +468,36 @@ def run_adjoint(args):
     cand = [(j, k) for j in range(1, ny - 1) for k in range(1, nz - 1)]
     pick = [cand[i] for i in rng.choice(len(cand), 16, replace=False)]
     hs = args.fd_step
+    # central differences with the configured step, and a noise check: J is
+    # computed with solves to a relative residual of 1e-12 whose rounding
+    # differs from run to run, so a difference quotient carries about
+    # |dJ_noise| / step of noise; the Richardson combination of steps 10 and
+    # 20 times larger, (4 D(10 h) - D(20 h)) / 3, removes the O(step^2)
+    # truncation term at a tenth of that noise
+    def cdiff(fn, h):
+        return (fn(h) - fn(-h)) / (2 * h)
+
+    def fds(fn):
+        d1, d10, d20 = cdiff(fn, hs), cdiff(fn, 10 * hs), cdiff(fn, 20 * hs)
+        return d1, (4 * d10 - d20) / 3
+
     rows = []
     for (j, k) in pick:
         idx = j * nz + k
-        p1, p2 = prof0.copy(), prof0.copy()
-        p1[idx] += hs
-        p2[idx] -= hs
-        fd = (J_of(p1, les_cases.CS) - J_of(p2, les_cases.CS)) / (2 * hs)
-        rows.append({"j": j, "k": k, "adjoint": float(g[idx]), "fd": fd,
-                     "rel_err": abs(fd - g[idx]) / max(abs(g[idx]), 1e-300)})
-    fdc = (J_of(prof0, les_cases.CS + hs) - J_of(prof0, les_cases.CS - hs)) / (2 * hs)
+
+        def Jp(h, idx=idx):
+            p = prof0.copy()
+            p[idx] += h
+            return J_of(p, les_cases.CS)
+        fd, fdr = fds(Jp)
+        rows.append({"j": j, "k": k, "adjoint": float(g[idx]), "fd": fd, "fd_richardson": fdr,
+                     "rel_err": abs(fd - g[idx]) / max(abs(g[idx]), 1e-300),
+                     "rel_err_richardson": abs(fdr - g[idx]) / max(abs(g[idx]), 1e-300)})
+    fdc, fdcr = fds(lambda h: J_of(prof0, les_cases.CS + h))
     cs_err = abs(fdc - gcs) / max(abs(gcs), 1e-300)
+    cs_err_r = abs(fdcr - gcs) / max(abs(gcs), 1e-300)
     errs = [r["rel_err"] for r in rows] + [cs_err]
+    errs_r = [r["rel_err_richardson"] for r in rows] + [cs_err_r]
     line = {"metric": "adjoint gradient of the probe-box kinetic energy vs central finite differences",
             "value": max(errs), "unit": "max relative error", "higher_is_better": False, "n_gpus": 1,
             "steps": nsteps, "warmup": 0, "dtype": "f32 inner / f64 outer (tol %g)" % args.adj_tol, "data": "synthetic",
@@ -487,7 +505,10 @@ def run_adjoint(args):
                                    "every 10, probe [96,120)x[16,48)x[16,48), controls 64x64 inlet u + Cs" % (nsteps, dt),
                        "fd_step": hs, "fd_entries": 16},
             "J": J, "grad_cs": gcs, "fd_cs": fdc, "cs_rel_err": cs_err, "grad_inlet_max_abs": float(np.abs(g).max()),
-            "median_rel_err": float(np.median(errs)), "entries": rows,
+            "median_rel_err": float(np.median(errs)),
+            "richardson": {"steps": [10 * hs, 20 * hs], "max_rel_err": max(errs_r),
+                           "median_rel_err": float(np.median(errs_r)), "cs_rel_err": cs_err_r},
+            "entries": rows,
             "forward_s": t_fwd, "backward_s": t_bwd, "backward_over_forward": t_bwd / t_fwd,
             "tangent": {"dJ": dJ_tl, "adjoint_projection": proj, "rel_err": tl_err, "seconds": t_tl}}
     print(json.dumps(line), flush=True)

@@ -83,7 +83,7 @@ __global__ void k_ic_build(Plane P, StencilView A, double* Lc, double* Lw, doubl
 
 // ---- pipelined wavefront -----------------------------------------------------
 #ifndef LES_WAVE_WB
-#define LES_WAVE_WB 8
+#define LES_WAVE_WB 4
 #endif
 #ifndef LES_WAVE_TJ
 #define LES_WAVE_TJ 4
