@@ -392,6 +392,9 @@ def run_batch(args):
                        "l2": "inputs (~%.1f GB) larger than L2" % (cells * 120 / 1e9),
                        "pdl": 0 if args.pdl is None else args.pdl, "phys32": args.phys32,
                        "form": "batched solves" if args.ens_batched else "one branch per case",
+                       "split": ("static: whole-length strips, then one more chunk for the longest march until "
+                                 "the items reach 4x the resident warps" if args.ens_batched else
+                                 "per case from the ensemble autotuner"),
                        "autotune_us_per_iteration": tune_us, "autotune_s": tune_s,
                        "first_steps_with_capture_s": warm_s},
             "gpu_launches": launches, "iters_inner_mean": statistics.mean(iters), "rel_residual_max": worst,
