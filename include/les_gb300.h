@@ -202,7 +202,9 @@ les_status les_pcg(les_ctx* ctx, const les_pcg_opts* opts, les_pcg_result* res);
 /* fast_apply_laplacian, src/pressure.cpp:709-746: out = A in. */
 les_status les_spmv(les_ctx* ctx, int in_slot, int out_slot);
 /* The preconditioner of opts applied once: out = M^-1 in
- * (src/pressure.cpp:420-428, :442-482, :851-906). */
+ * (src/pressure.cpp:420-428, :442-482, :851-906).  With an IC preconditioner
+ * the call waits for the wavefront and returns LES_TIMEOUT if one of its
+ * bounded waits gave up. */
 les_status les_precond_apply(les_ctx* ctx, const les_pcg_opts* opts, int in_slot, int out_slot);
 /* parallel_dot, src/pressure.cpp:962-970. */
 les_status les_dot(les_ctx* ctx, int a_slot, int b_slot, double* out);
@@ -366,10 +368,16 @@ typedef enum les_option {
                              passes are launched as programmatic dependents of the
                              kernel before them (their blocks become resident while it
                              drains); 0: plain stream order */
-    LES_OPT_PHYS32 = 8    /* 1 (default): a les_step whose pressure solve is the
+    LES_OPT_PHYS32 = 8,   /* 1 (default): a les_step whose pressure solve is the
                              mixed-precision PCG computes nu_t and the momentum update
                              in FP32 (FP64 fields, FP64 velocity update; not with
                              want_tau); 0: the reference-order FP64 kernels */
+    LES_OPT_TEST_STALL = 9 /* test hook, 0 (default) off.  1: the first tile of the
+                             IC(0) and GS-SOR wavefronts withholds its progress, so
+                             the tiles after it wait in vain until their bounded wait
+                             (about 2 s) gives up; the solve then returns LES_TIMEOUT
+                             and the context stays usable.  For testing the failure
+                             path only. */
 } les_option;
 les_status les_set_option(les_ctx* ctx, int option, int value);
 

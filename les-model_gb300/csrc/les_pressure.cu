@@ -829,7 +829,10 @@ les_status les_precond_apply(les_ctx* c, const les_pcg_opts* o, int in, int out)
         les_status st = ensure_stored_A(c);
         if (st) return st;
     }
-    return precond_dev(c, o, c->slot[in], c->slot[out], 0);
+    les_status st = precond_dev(c, o, c->slot[in], c->slot[out], 0);
+    if (!st && (o->precond == LES_PC_IC || o->precond == LES_PC_IC_A))
+        st = wave_check(c);   // waits for the wavefront: LES_TIMEOUT if a bounded wait gave up
+    return st;
 }
 
 les_status les_pcg(les_ctx* c, const les_pcg_opts* o, les_pcg_result* res)

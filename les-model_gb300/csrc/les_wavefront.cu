@@ -102,6 +102,7 @@ struct Wave {
     int steps;                 // marching steps of a tile: planes + 31 lane skews + TJ-1 row skews
     int* prog;                 // progress counter per tile
     int* err;                  // set by a wait that gives up
+    int stall;                 // tile that withholds its progress (LES_OPT_TEST_STALL), or -1
 };
 
 __device__ __forceinline__ int ld_acquire(const int* p)
@@ -316,7 +317,7 @@ __device__ bool ic_tile(const Wave& W, int t, int base, const T* __restrict__ Lc
             sg.xs[tau & 1][w][lane] = out;
             __syncthreads();          // the next step reads this step's rows
         }
-        publish(W.prog + t, base + tend);
+        if (t != W.stall) publish(W.prog + t, base + tend);   // block-uniform
     }
     cp_wait<0>();
     return true;
@@ -431,7 +432,7 @@ __device__ bool gs_tile(const Wave& W, int t, int base, double d2x, double d2y, 
             sg.xs[tau & 1][w][lane] = v;
             __syncthreads();          // the next step reads this step's rows
         }
-        publish(W.prog + t, base + tend);
+        if (t != W.stall) publish(W.prog + t, base + tend);   // block-uniform
     }
     cp_wait<0>();
     return true;
@@ -631,6 +632,7 @@ les_status wave_setup(les_ctx* c, int nx, int ny, int nz, int off, int span, Wav
     c->wave_epoch += span + 1;
     W.prog = c->wave_prog;
     W.err = (int*)(c->gsync + 2);
+    W.stall = c->test_stall ? 0 : -1;
     return LES_OK;
 }
 

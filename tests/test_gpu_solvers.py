@@ -270,3 +270,59 @@ def test_mixed_column_solve_stops_at_the_iteration_cap(cap):
         x = c.download("p")
     assert st == G.NOT_CONVERGED and r.iters == cap, (st, r.iters)
     assert np.isfinite(r.residual) and np.all(np.isfinite(x))
+
+
+def test_wavefront_wait_gives_up_and_the_context_recovers(oracle_lib):
+    """Failure path of the pipelined wavefronts, without a GPU fault: with
+    LES_OPT_TEST_STALL the first tile withholds its progress, so the tiles
+    after it wait on a counter that nothing advances until their bounded
+    wait (about 2 s) gives up.  The IC(0)-preconditioned PCG, the IC apply
+    and GS-SOR then return LES_TIMEOUT, and with the option off the same
+    context computes the reference's results bit for bit again."""
+    import time
+
+    shape, h = (24, 40, 36), 1.0 / 16   # several tiles along j and k
+    m = G.Mesh(*shape, h, h, h)
+    om = O.Mesh(*shape, h, h, h)
+    n = m.n
+    rng = np.random.default_rng(8)
+    solid = np.zeros(n, np.uint8)
+    u, v, w = (rng.uniform(-1, 1, n) for _ in range(3))
+    p0 = rng.uniform(-1, 1, n)
+    r = rng.uniform(-1, 1, n)
+    A = oracle_lib.build_stencil(om, solid)
+    L = oracle_lib.ic_build(om, A)
+    with G.Context(m) as c:
+        c.upload_mask(solid)
+        c.build_stencil()
+        c.build_ic()
+        ic = G.pcg_opts(precond=G.PC_IC, max_iter=3)
+        c.set_option(G.OPT_TEST_STALL, 1)
+        t0 = time.perf_counter()
+        c.upload("b", r)
+        with pytest.raises(G.LesError) as e:
+            c.precond_apply(ic, "b", "p_rhs")
+        assert e.value.status == G.TIMEOUT
+        c.upload("p", np.zeros(n))
+        with pytest.raises(G.LesError) as e:
+            c.pcg(ic)
+        assert e.value.status == G.TIMEOUT
+        for k, a in (("u", u), ("v", v), ("w", w), ("p", p0)):
+            c.upload(k, a)
+        with pytest.raises(G.LesError) as e:
+            c.solve_gs(1e-4, 1.2, 5, 1.7, 0.0)
+        assert e.value.status == G.TIMEOUT
+        assert time.perf_counter() - t0 < 60
+        # the same context, option off: bit-exact again
+        c.set_option(G.OPT_TEST_STALL, 0)
+        c.upload("b", r)
+        c.precond_apply(ic, "b", "p_rhs")
+        z = np.zeros(n)
+        oracle_lib.ic_apply(om, L, r, z)
+        assert np.array_equal(c.download("p_rhs"), z)
+        c.upload("p", p0)
+        sweeps = c.solve_gs(1e-4, 1.2, 5, 1.7, 0.0)
+        pr = p0.copy()
+        it = oracle_lib.solve_gs(om, 1e-4, 1.2, u, v, w, pr, solid, 5, 1.7, 0.0)
+        assert sweeps == it == 5
+        assert np.array_equal(c.download("p"), pr)
