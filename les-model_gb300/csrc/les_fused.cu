@@ -393,7 +393,7 @@ __global__ void __launch_bounds__(NT) k_pass_a_tma(Geo g, ViewF A, int CI, const
             const int s = P % A2_RING;
             if (!mbar_wait_bounded(&bar[s], (phase >> s) & 1u)) {
                 tma_timeout(st);
-                mbar_wait_bounded(&bar[s], (phase >> s) & 1u);   // let a late copy land before leaving
+                mbar_drain(bar, phase, A2_RING, P, 2, Pend);   // late copies land before leaving
                 return;
             }
             phase ^= 1u << s;
@@ -534,7 +534,7 @@ __global__ void __launch_bounds__(NT) k_pass_b_tma(Geo g, ViewF A, int CI, ChebF
             const int s = I % TB::RING;
             if (!mbar_wait_bounded(&bar[s], (phase >> s) & 1u)) {
                 tma_timeout(st);
-                mbar_wait_bounded(&bar[s], (phase >> s) & 1u);   // let a late copy land before leaving
+                mbar_drain(bar, phase, TB::RING, I, 2, Iend);   // late copies land before leaving
                 return;
             }
             phase ^= 1u << s;

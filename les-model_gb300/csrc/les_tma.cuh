@@ -51,6 +51,21 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity
     return false;
 }
 
+// After a wait on the plane `cur` gave up: waits again (bounded) on every
+// ring slot whose copy was issued -- planes cur .. min(cur + ahead, last) --
+// so that a late copy lands before the CTA leaves and its shared memory is
+// handed to another CTA.  `phase` bit s is the parity the next wait on slot
+// s expects.  If these bounded waits also give up, the copy never completes
+// and the CTA leaves anyway: an unbounded wait there would hang the GPU.  The
+// TMA-staged passes are off by default (LES_OPT_TMA).
+__device__ __forceinline__ void mbar_drain(uint64_t* bar, unsigned phase, int ring, int cur, int ahead, int last)
+{
+    for (int q = 0; q <= ahead && cur + q <= last; ++q) {
+        const int s = (cur + q) % ring;
+        mbar_wait_bounded(&bar[s], (phase >> s) & 1u);
+    }
+}
+
 // 3-D tiled TMA load of the box at element coordinates (x, y, z) into shared
 // memory; completion is signalled on `bar` as transaction bytes.  x times
 // the element size must be a multiple of 16 bytes; coordinates outside the
