@@ -931,9 +931,10 @@ les_status inner_solve_fused(les_ctx* c, const les_pcg_opts* o, ViewF A, SolverS
 // ---- the whole mixed solve as a CUDA graph -----------------------------------
 // Both loops run on the device: each is a conditional `while` node whose body
 // ends with a one-thread kernel that sets the loop's condition from the
-// solver state.  The inner body holds two iterations so that the ping-pong
-// buffers are in the same roles every time it repeats (kernels of an
-// iteration that starts after convergence exit at once).
+// solver state.  The inner body holds 2 * INNER_BODY_PAIRS iterations (an
+// even number, so that the ping-pong buffers are in the same roles every time
+// it repeats; kernels of an iteration that starts after convergence exit at
+// once).
 
 __global__ void k_cond_inner(const SolverState* in, cudaGraphConditionalHandle h, int cap)
 {
@@ -986,10 +987,12 @@ les_status capture_mixed_fused(les_ctx* c, const les_pcg_opts* o, ViewF A, int k
         if ((s2 = emit_pass_b(c, P, false, 1, 1))) return s2;         //   r1 -> r0
         s2 = capture_while(c, set_inner, [&](cudaGraphConditionalHandle hi) -> les_status {
             les_status s3;
-            if ((s3 = emit_pass_a(c, P, false, 1))) return s3;        // p1 -> p0
-            if ((s3 = emit_pass_b(c, P, false, 0, 0))) return s3;     // r0 -> r1
-            if ((s3 = emit_pass_a(c, P, false, 0))) return s3;        // p0 -> p1
-            if ((s3 = emit_pass_b(c, P, false, 1, 1))) return s3;     // r1 -> r0
+            for (int q = 0; q < INNER_BODY_PAIRS; ++q) {
+                if ((s3 = emit_pass_a(c, P, false, 1))) return s3;    // p1 -> p0
+                if ((s3 = emit_pass_b(c, P, false, 0, 0))) return s3; // r0 -> r1
+                if ((s3 = emit_pass_a(c, P, false, 0))) return s3;    // p0 -> p1
+                if ((s3 = emit_pass_b(c, P, false, 1, 1))) return s3; // r1 -> r0
+            }
             return set_inner(hi);
         });
         if (s2) return s2;

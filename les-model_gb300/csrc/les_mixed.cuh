@@ -163,6 +163,16 @@ les_status inner_solve_fused(les_ctx* c, const les_pcg_opts* o, ViewF A, SolverS
 // cases of an ensemble: each batched kernel covers every case, its blocks
 // split into consecutive per-case ranges (prefix arrays of block starts), and
 // each block works on its own case only.  Lives in device memory.
+// Iteration pairs per pass of the inner loop body of a captured mixed solve:
+// each pass of a conditional loop costs about 6 us at 256x128x128 (the
+// condition kernel and the body's relaunch), each iteration that starts
+// after convergence a few us of early exits.  Measured, 20 steps of
+// 256x128x128: 1 pair 140.4, 2 pairs 144.0, 3 pairs 145.5, 4 pairs 146.1
+// Mcell-steps/s; 512x256x256 unchanged.
+#ifndef INNER_BODY_PAIRS
+#define INNER_BODY_PAIRS 4
+#endif
+
 struct BatchCase {
     Geo g;
     ColMap ma, mb;                 // column-pass work splits

@@ -97,10 +97,12 @@ unsigned long long graph_step_stats(les_ctx* c, const les_step_params* prm, unsi
     s.b_norm = o.bnorm;
     s.status = o.done ? (les_status)o.status : LES_NOT_CONVERGED;
     if (stats) *stats = s;
-    // less one pass of each loop body (13 nodes), plus 8 kernels per outer
-    // correction and 5 per pass of the two-iteration inner body
-    const long long body = (o.iters - o.k + 1) / 2;
-    const long long run = (long long)captured - 13 + 8LL * o.k + 5LL * (body > 0 ? body : 0);
+    // less one pass of each loop body, plus 8 kernels per outer correction
+    // and 4 * INNER_BODY_PAIRS + 1 per pass of the inner body (passes counted
+    // approximately: a correction's first iteration is outside the loop)
+    const long long per = 4LL * INNER_BODY_PAIRS + 1, len = 2LL * INNER_BODY_PAIRS;
+    const long long body = (o.iters - o.k + (len / 2) * o.k) / len;
+    const long long run = (long long)captured - (8 + per) + 8LL * o.k + per * (body > 0 ? body : 0);
     return run > 0 ? (unsigned long long)run : captured;
 }
 
