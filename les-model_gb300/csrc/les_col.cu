@@ -54,8 +54,18 @@ using namespace les;
 
 namespace {
 
-constexpr int CT = 128;          // threads per block: 4 independent warps
-constexpr int CWPB = CT / 32;
+// Block shapes.  A pass's deferred head sums every block partial of the
+// pass before it, so fewer, larger blocks make the head cheaper: a
+// single-case kernel that fits an even number of 4-warp blocks on an SM runs
+// half as many 8-warp blocks instead (256x128x128: 146.3 Mcell-steps/s with
+// 4-warp blocks, 149.1 with 8; 512x256x256: 107.9 and 107.2).  The batched
+// kernels sum their partials in a separate kernel and keep 4 warps.
+constexpr int col_threads(int blocks4) { return blocks4 % 2 == 0 ? 256 : 128; }
+constexpr int col_blocks(int blocks4) { return blocks4 % 2 == 0 ? blocks4 / 2 : blocks4; }
+constexpr int blocks4_a(int TJ) { return TJ == 8 ? 4 : 2; }               // 4-warp blocks per SM
+constexpr int blocks4_b(int S, int TJ) { return (TJ == 4 && S <= 3) ? 3 : 2; }
+constexpr int CTB = 128;          // batched kernels: threads per block
+constexpr int CWPB_B = CTB / 32;
 constexpr unsigned FULL = 0xffffffffu;
 
 struct Coef {
@@ -385,7 +395,7 @@ __device__ __forceinline__ void col_a(const Geo& g, const ColMap& m, const Coef&
     constexpr int H = TJ + 2;
     __shared__ double sm[64];
     const int lane = threadIdx.x & 31;
-    const int item = blk * CWPB + (threadIdx.x >> 5);
+    const int item = blk * (int)(blockDim.x >> 5) + (threadIdx.x >> 5);
     const StripPos s = strip_pos<1, TJ>(g, m, item, lane);   // from the arguments only
     dep_wait();
     float beta = 0.f;
@@ -516,7 +526,7 @@ __device__ __forceinline__ void col_a(const Geo& g, const ColMap& m, const Coef&
 }
 
 template <int TJ, bool FIRST>
-__global__ void __launch_bounds__(CT, TJ == 8 ? 4 : 2) k_col_a(Geo g, ColMap m, Coef k, const float* __restrict__ z,
+__global__ void __launch_bounds__(col_threads(blocks4_a(TJ)), col_blocks(blocks4_a(TJ))) k_col_a(Geo g, ColMap m, Coef k, const float* __restrict__ z,
                                                              const float* __restrict__ pold, float* __restrict__ pnew,
                                                              float* __restrict__ q, float* __restrict__ e,
                                                              double* partials, unsigned* counter, SolverState* st,
@@ -569,7 +579,7 @@ __device__ __forceinline__ void col_b(const Geo& g, const ColMap& m, const ColCh
     constexpr int NL = S > 1 ? S - 1 : 1;   // stored levels z_1 .. z_{S-1}
     __shared__ double sm[64];
     const int lane = threadIdx.x & 31;
-    const int item = blk * CWPB + (threadIdx.x >> 5);
+    const int item = blk * (int)(blockDim.x >> 5) + (threadIdx.x >> 5);
     const StripPos s = strip_pos<S, TJ>(g, m, item, lane);   // from the arguments only
     dep_wait();
     float alpha = 0.f;
@@ -727,7 +737,7 @@ __device__ __forceinline__ void col_b(const Geo& g, const ColMap& m, const ColCh
 }
 
 template <int S, int TJ, bool FIRST>
-__global__ void __launch_bounds__(CT, (TJ == 4 && S <= 3) ? 3 : 2) k_col_b(Geo g, ColMap m, ColCheb c3, float inv_c0,
+__global__ void __launch_bounds__(col_threads(blocks4_b(S, TJ)), col_blocks(blocks4_b(S, TJ))) k_col_b(Geo g, ColMap m, ColCheb c3, float inv_c0,
                                                const float* __restrict__ r_in, float* __restrict__ r_out,
                                                const float* __restrict__ q, float* __restrict__ z_out,
                                                double* partials, unsigned* counter, SolverState* st,
@@ -755,7 +765,7 @@ __global__ void k_x_update(Geo g, double* __restrict__ x, const float* __restric
 // fields take registers that the single-case kernel reads from its
 // parameters, and 4 blocks would spill.)
 template <int TJ, bool FIRST>
-__global__ void __launch_bounds__(CT, TJ == 8 ? 3 : 2) k_col_a_batch(const BatchCase* __restrict__ cs,
+__global__ void __launch_bounds__(CTB, TJ == 8 ? 3 : 2) k_col_a_batch(const BatchCase* __restrict__ cs,
                                                                    const int* __restrict__ pre, int n, int pc)
 {
     const int c = batch_case(pre, n, blockIdx.x);
@@ -767,7 +777,7 @@ __global__ void __launch_bounds__(CT, TJ == 8 ? 3 : 2) k_col_a_batch(const Batch
 }
 
 template <int S, int TJ, bool FIRST>
-__global__ void __launch_bounds__(CT, (TJ == 4 && S <= 3) ? 3 : 2) k_col_b_batch(const BatchCase* __restrict__ cs,
+__global__ void __launch_bounds__(CTB, blocks4_b(S, TJ)) k_col_b_batch(const BatchCase* __restrict__ cs,
                                                                                const int* __restrict__ pre, int n,
                                                                                int rin)
 {
@@ -829,10 +839,13 @@ bool valid_tj_b(int S, int tj)
     return tj == 4;
 }
 
+int threads_a(int tj) { return col_threads(blocks4_a(tj)); }
+int threads_b(int S, int tj) { return col_threads(blocks4_b(S, tj)); }
+
 // Strips x chunks for one pass: as many chunks along i as fit in one wave of
 // resident warps (a partial second wave would double the pass time); a
 // chunk re-reads 2 x halo planes.
-ColMap col_map(les_ctx* c, const void* fn, int halo, int tj, int ci_force)
+ColMap col_map(les_ctx* c, const void* fn, int threads, int halo, int tj, int ci_force)
 {
     const Geo& g = c->g;
     ColMap m{};
@@ -844,9 +857,9 @@ ColMap col_map(les_ctx* c, const void* fn, int halo, int tj, int ci_force)
     int ci = ci_force;
     if (ci <= 0) {
         int occ = 1;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, CT, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, 0);
         const double share = c->share > 0 && c->share <= 1 ? c->share : 1.0;
-        const long long warps = (long long)((occ < 1 ? 1 : occ) * CWPB * c->sms * share);
+        const long long warps = (long long)((occ < 1 ? 1 : occ) * (threads / 32) * c->sms * share);
         long long chunks = warps / tiles;
         if (chunks < 1) chunks = 1;
         ci = (int)((g.nx + chunks - 1) / chunks);
@@ -913,10 +926,11 @@ les_status col_plan(les_ctx* c, const les_pcg_opts* o, ViewF A, SolverState* in,
     P.cap = o->max_iter;
     const int tja = (c->tune_tja == 8 || c->tune_tja == 16) ? c->tune_tja : 8;
     const int tjb = valid_tj_b(P.S, c->tune_tjb) ? c->tune_tjb : default_tj_b(P.S);
-    P.ma = col_map(c, (const void*)pick_a(tja, false), 1, tja, c->tune_cia);
-    P.mb = col_map(c, (const void*)pick_b(P.S, tjb, false), P.S, tjb, c->tune_cib);
-    P.blocks_a = (P.ma.items + CWPB - 1) / CWPB;
-    P.blocks_b = (P.mb.items + CWPB - 1) / CWPB;
+    const int wa = threads_a(tja) / 32, wb = threads_b(P.S, tjb) / 32;
+    P.ma = col_map(c, (const void*)pick_a(tja, false), threads_a(tja), 1, tja, c->tune_cia);
+    P.mb = col_map(c, (const void*)pick_b(P.S, tjb, false), threads_b(P.S, tjb), P.S, tjb, c->tune_cib);
+    P.blocks_a = (P.ma.items + wa - 1) / wa;
+    P.blocks_b = (P.mb.items + wb - 1) / wb;
     // pass B's partials (2 per block) then pass A's, both live across a pass
     if ((size_t)2 * P.blocks_b + (size_t)P.blocks_a > c->partials_len)
         return fail(c, LES_BAD_ARG, "column pass grid exceeds the reduction scratch");
@@ -930,7 +944,7 @@ les_status col_pass_a(les_ctx* c, const ColPlan& P, bool first, int pc)
     float *z = c->f[1], *pb[2] = {c->f[2], c->f[3]}, *q = c->f[4], *e = c->f[5];
     float2* const part = reinterpret_cast<float2*>(c->partials);   // pass B's pairs, then pass A's
     const Defer df{part, P.blocks_b, part + 2 * (size_t)P.blocks_b};
-    launch_pdl(c, PROF_IN_SPMV, pick_a(P.ma.tj, first), P.blocks_a, CT, c->g, P.ma, coef_of(P), (const float*)z,
+    launch_pdl(c, PROF_IN_SPMV, pick_a(P.ma.tj, first), P.blocks_a, threads_a(P.ma.tj), c->g, P.ma, coef_of(P), (const float*)z,
              (const float*)pb[pc], pb[pc ^ 1], q, e, c->partials, c->counters + 15, P.in, pc ^ 1, df, P.out, P.cap);
     return check_launch(c, "column pass A");
 }
@@ -941,7 +955,7 @@ les_status col_pass_b(les_ctx* c, const ColPlan& P, bool first, int rin)
     float *z = c->f[1], *q = c->f[4];
     float2* const part = reinterpret_cast<float2*>(c->partials);
     const Defer df{part + 2 * (size_t)P.blocks_b, P.blocks_a, part};
-    launch_pdl(c, PROF_IN_CHEB, pick_b(P.S, P.mb.tj, first), P.blocks_b, CT, c->g, P.mb, P.c3, P.inv_c0,
+    launch_pdl(c, PROF_IN_CHEB, pick_b(P.S, P.mb.tj, first), P.blocks_b, threads_b(P.S, P.mb.tj), c->g, P.mb, P.c3, P.inv_c0,
              (const float*)r[rin], r[rin ^ 1], (const float*)q, z, c->partials, c->counters + 14, P.in, P.out, P.cap,
              df);
     return check_launch(c, "column pass B");
@@ -969,33 +983,35 @@ static KAB pick_b_batch(int S, bool first)
 
 int col_batch_tj_b(int S) { return default_tj_b(S); }
 
+int col_batch_warps_per_block() { return CWPB_B; }
+
 ColMap col_batch_map(les_ctx* c, int pass, int S, int chunk_planes)
 {
-    if (pass == 0) return col_map(c, (const void*)pick_a_batch(false), 1, 8, chunk_planes);
-    return col_map(c, (const void*)pick_b_batch(S, false), S, default_tj_b(S), chunk_planes);
+    if (pass == 0) return col_map(c, (const void*)pick_a_batch(false), CTB, 1, 8, chunk_planes);
+    return col_map(c, (const void*)pick_b_batch(S, false), CTB, S, default_tj_b(S), chunk_planes);
 }
 
 int col_batch_resident_warps(int pass, int S)
 {
     int occ = 1, dev = 0, sms = 1;
     const void* fn = pass == 0 ? (const void*)pick_a_batch(false) : (const void*)pick_b_batch(S, false);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, CT, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, CTB, 0);
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    return (occ < 1 ? 1 : occ) * CWPB * sms;
+    return (occ < 1 ? 1 : occ) * CWPB_B * sms;
 }
 
 les_status col_batch_pass_a(cudaStream_t s, bool first, int pc, const BatchCase* cs, const int* pre, int n,
                             int blocks)
 {
-    pick_a_batch(first)<<<blocks, CT, 0, s>>>(cs, pre, n, pc);
+    pick_a_batch(first)<<<blocks, CTB, 0, s>>>(cs, pre, n, pc);
     return cudaPeekAtLastError() == cudaSuccess ? LES_OK : LES_CUDA_ERROR;
 }
 
 les_status col_batch_pass_b(cudaStream_t s, int S, bool first, int rin, const BatchCase* cs, const int* pre, int n,
                             int blocks)
 {
-    pick_b_batch(S, first)<<<blocks, CT, 0, s>>>(cs, pre, n, rin);
+    pick_b_batch(S, first)<<<blocks, CTB, 0, s>>>(cs, pre, n, rin);
     return cudaPeekAtLastError() == cudaSuccess ? LES_OK : LES_CUDA_ERROR;
 }
 

@@ -245,7 +245,9 @@ les_status batch_plan(les_ensemble* e, const les_step_params* prm, les_ensemble:
         C.inner_cap = o.inner_max_iter > 0 ? o.inner_max_iter : o.max_iter;
         C.max_outer = o.max_outer > 0 ? o.max_outer : 50;
         C.act = 0;
-        const int nb[4] = {(ma[i].items + 3) / 4, (mb[i].items + 3) / 4, batch_resid_blocks(c->g), (c->g.n + 255) / 256};
+        const int wpb = col_batch_warps_per_block();
+        const int nb[4] = {(ma[i].items + wpb - 1) / wpb, (mb[i].items + wpb - 1) / wpb, batch_resid_blocks(c->g),
+                           (c->g.n + 255) / 256};
         if ((size_t)2 * nb[0] > c->partials_len || (size_t)2 * nb[1] > c->partials_len ||
             (size_t)nb[2] > c->partials_len)
             return efail(e, LES_BAD_ARG, "case " + std::to_string(i) + ": batched grid exceeds the reduction scratch");

@@ -206,6 +206,7 @@ __device__ __forceinline__ int batch_case(const int* pre, int n, int block)
 
 // column passes over all cases (S levels; rows as in the single-case default)
 int col_batch_tj_b(int S);
+int col_batch_warps_per_block();   // warps of a batched column-pass block (one item each)
 ColMap col_batch_map(les_ctx* c, int pass, int S, int chunk_planes);   // pass 0: A, 1: B
 int col_batch_resident_warps(int pass, int S);
 les_status col_batch_pass_a(cudaStream_t s, bool first, int pc, const BatchCase* cs, const int* pre, int n,
