@@ -372,12 +372,16 @@ typedef enum les_option {
                              mixed-precision PCG computes nu_t and the momentum update
                              in FP32 (FP64 fields, FP64 velocity update; not with
                              want_tau); 0: the reference-order FP64 kernels */
-    LES_OPT_TEST_STALL = 9 /* test hook, 0 (default) off.  1: the first tile of the
+    LES_OPT_TEST_STALL = 9, /* test hook, 0 (default) off.  1: the first tile of the
                              IC(0) and GS-SOR wavefronts withholds its progress, so
                              the tiles after it wait in vain until their bounded wait
                              (about 2 s) gives up; the solve then returns LES_TIMEOUT
                              and the context stays usable.  For testing the failure
                              path only. */
+    LES_OPT_COL_STRIDE = 10 /* 1 (default): the register-column passes of a grid with
+                             nz = 32, 64, 128 or 256 run kernels compiled for that row
+                             stride (row offsets as immediates); 0: the kernels that
+                             read the stride at run time.  Same results either way. */
 } les_option;
 les_status les_set_option(les_ctx* ctx, int option, int value);
 

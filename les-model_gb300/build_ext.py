@@ -29,6 +29,10 @@ UNITS = {
     "les_mixed.cu": [],
     "les_fused.cu": [],
     "les_col.cu": [],
+    "les_col_sj32.cu": [],
+    "les_col_sj64.cu": [],
+    "les_col_sj128.cu": [],
+    "les_col_sj256.cu": [],
     "les_ensemble.cu": [],
     "les_tune.cu": [],
     "les_adjoint.cu": ["-fmad=false"],

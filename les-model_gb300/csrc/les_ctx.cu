@@ -412,6 +412,7 @@ les_status les_set_option(les_ctx* c, int option, int value)
     case LES_OPT_PDL: c->pdl = value ? 1 : 0; return LES_OK;
     case LES_OPT_PHYS32: c->phys32 = value ? 1 : 0; return LES_OK;
     case LES_OPT_TEST_STALL: c->test_stall = value ? 1 : 0; return LES_OK;
+    case LES_OPT_COL_STRIDE: c->col_stride = value ? 1 : 0; return LES_OK;
     case LES_OPT_FUSED: c->fused = value == 2 ? 2 : (value ? 1 : 0); return LES_OK;
     case LES_OPT_TMA: c->opt_tma = value ? 1 : 0; return LES_OK;
     case LES_OPT_ROWS_A: c->tune_tja = value; return LES_OK;

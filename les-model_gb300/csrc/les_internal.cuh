@@ -329,6 +329,7 @@ struct les_ctx {
     int pdl = 1;                          // LES_OPT_PDL
     int phys32 = 1;                       // LES_OPT_PHYS32
     int test_stall = 0;                   // LES_OPT_TEST_STALL
+    int col_stride = 1;                   // LES_OPT_COL_STRIDE
     cudaStream_t aux = nullptr;           // capture stream for conditional-loop bodies
     struct les::StepGraph* sg[2] = {};
     int sg_last = 0;                      // slot of the graph launched last

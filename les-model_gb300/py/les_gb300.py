@@ -25,7 +25,7 @@ SOLVER_PCG, SOLVER_JACOBI, SOLVER_GS = 0, 1, 2
 PC_JACOBI, PC_IC, PC_CHEBYSHEV, PC_IC_A = 0, 1, 2, 3
 FP64, MIXED = 0, 1
 (OPT_FUSED, OPT_TMA, OPT_ROWS_A, OPT_ROWS_B, OPT_CHUNK_A, OPT_CHUNK_B, OPT_GRAPH, OPT_PDL, OPT_PHYS32,
- OPT_TEST_STALL) = range(10)
+ OPT_TEST_STALL, OPT_COL_STRIDE) = range(11)
 DIAGS = ("c", "n", "s", "e", "w", "t", "b")
 
 _dp = C.POINTER(C.c_double)

@@ -250,6 +250,63 @@ def test_tma_fused_matches_plain_fused(shape, pc, deg):
     assert maxrel(t[4], u[4]) < 1e-6, maxrel(t[4], u[4])
 
 
+def _mixed_solve(m, b, lmax, pc, deg, max_iter, options):
+    tol = 1e-8 * np.linalg.norm(b)
+    with G.Context(m) as c:
+        for opt, val in options:
+            c.set_option(opt, val)
+        c.upload_mask(np.zeros(m.n, np.uint8))
+        c.build_stencil()
+        c.upload("b", b)
+        c.upload("p", np.zeros(m.n))
+        st, r = c.pcg(G.pcg_opts(precond=pc, max_iter=max_iter, tol=tol, lambda_min=3 * np.pi ** 2,
+                                 lambda_max=lmax, degree=max(deg, 1), precision=G.MIXED, inner_rtol=1e-4))
+        return st, r.iters, r.outer, r.residual, c.download("p")
+
+
+@pytest.mark.parametrize("fused", [1, 2], ids=["columns", "tiles"])
+def test_single_level_chebyshev_follows_unfused(fused):
+    """Chebyshev degree 2 (one stencil level; the column pass keeps three
+    planes of r' for it) does not converge on these non-symmetric systems in
+    any form of the inner iteration, so the fused passes are checked against
+    the one-kernel-per-operation path over the first 12 inner iterations: the
+    same iterate to FP32 rounding."""
+    m, b, lmax = _odd_system((45, 37, 70), 154)
+    f = _mixed_solve(m, b, lmax, G.PC_CHEBYSHEV, 2, 12, [(G.OPT_FUSED, fused)])
+    u = _mixed_solve(m, b, lmax, G.PC_CHEBYSHEV, 2, 12, [(G.OPT_FUSED, 0)])
+    assert f[0] == u[0] == G.NOT_CONVERGED and f[1] == u[1] == 12, (f[:4], u[:4])
+    assert np.all(np.isfinite(f[4]))
+    assert maxrel(f[4], u[4]) < 1e-4, maxrel(f[4], u[4])
+
+
+@pytest.mark.parametrize("shape", [(40, 21, 32), (24, 17, 64), (20, 15, 128), (20, 15, 256)],
+                         ids=["nz32", "nz64", "nz128", "nz256"])
+@pytest.mark.parametrize("pc,deg,rows", [(G.PC_CHEBYSHEV, 4, (0, 0)), (G.PC_CHEBYSHEV, 4, (16, 4)),
+                                         (G.PC_CHEBYSHEV, 3, (8, 8)), (G.PC_CHEBYSHEV, 2, (8, 4)),
+                                         (G.PC_CHEBYSHEV, 5, (0, 0)), (G.PC_CHEBYSHEV, 7, (0, 0)),
+                                         (G.PC_JACOBI, 0, (0, 0))],
+                         ids=["cheb4", "cheb4-rows16x4", "cheb3-rows8x8", "cheb2-rows8x4", "cheb5", "cheb7",
+                              "jacobi"])
+def test_compiled_row_strides_match_runtime_stride(shape, pc, deg, rows):
+    """Grids with nz = 32, 64, 128 or 256 run the register-column kernels
+    compiled for that row stride (LES_OPT_COL_STRIDE 1, the default); they do
+    the arithmetic of the runtime-stride kernels in the same order, so the
+    solve is bit-identical: same status, inner and outer iteration counts and
+    pressure, for every strip shape (degree 2, which does not converge here,
+    over its first 12 inner iterations)."""
+    m, b, lmax = _odd_system(shape, sum(shape) + deg)
+    cap = 12 if deg == 2 else 20000
+    res = {}
+    for stride in (1, 0):
+        res[stride] = _mixed_solve(m, b, lmax, pc, deg, cap,
+                                   [(G.OPT_FUSED, 1), (G.OPT_COL_STRIDE, stride), (G.OPT_ROWS_A, rows[0]),
+                                    (G.OPT_ROWS_B, rows[1])])
+    a, z = res[1], res[0]
+    assert a[0] == (G.NOT_CONVERGED if deg == 2 else G.OK), a[:4]
+    assert a[:4] == z[:4], (a[:4], z[:4])
+    assert np.array_equal(a[4], z[4])
+
+
 @pytest.mark.parametrize("cap", [1, 2, 7])
 def test_mixed_column_solve_stops_at_the_iteration_cap(cap):
     """The register-column passes judge an inner iteration in the pass after
