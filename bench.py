@@ -561,6 +561,8 @@ def run_ours(args):
     if (not gs and args.tune and args.fused == 1 and args.rows == "0,0" and args.chunks == "0,0"
             and args.precond != "ic"):
         tune_us = ctx.autotune(prm.pcg)
+    shape_used = {k: ctx.get_option(o) for k, o in (("rows_a", G.OPT_ROWS_A), ("rows_b", G.OPT_ROWS_B),
+                                                    ("chunk_a", G.OPT_CHUNK_A), ("chunk_b", G.OPT_CHUNK_B))}
     ctx64 = ctxT = None
     if not gs and not args.no_fp64:   # the plain FP64 path on the same trajectory (the reference's arithmetic)
         ctx64, _ = make_ctx(G, les_cases, shape, h, solid, f, dev, args.precond)
@@ -706,7 +708,7 @@ def run_ours(args):
                        "inner_rtol": args.inner_rtol, "tma": args.tma, "fused": args.fused,
                        "rows": args.rows, "chunks": args.chunks, "graph": args.graph,
                        "pdl": 1 if args.pdl is None else args.pdl, "phys32": args.phys32,
-                       "autotune_us": tune_us},
+                       "autotune_us": tune_us, "strip_shape": shape_used},
             "e2e": e2e, "gpu_launches": launches, "wall_s": wall,
             "iters_mean": statistics.mean(rec["iters"]), "outer_mean": statistics.mean(rec["outer"]),
             "roofline": roof, "clocks": clk}

@@ -384,6 +384,10 @@ typedef enum les_option {
                              read the stride at run time.  Same results either way. */
 } les_option;
 les_status les_set_option(les_ctx* ctx, int option, int value);
+/* The current value of an option: the last one set, the default, or for the
+ * strip shapes (LES_OPT_ROWS_A/B, LES_OPT_CHUNK_A/B) what les_autotune chose
+ * (0 = the built-in choice). */
+les_status les_get_option(const les_ctx* ctx, int option, int* value);
 
 /* ---- accounting (no reference counterpart) ------------------------------ */
 /* Number of kernels this context has launched so far. */

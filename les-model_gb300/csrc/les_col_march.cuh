@@ -316,7 +316,9 @@ __device__ __noinline__ HeadOut head_a(const float2* __restrict__ pin, int nb_in
             if (err < st->tol) status = LES_OK;
             else if (!isfinite(err)) status = LES_NONFINITE;
             else if (kk >= st->max_iter || total >= total_cap) status = LES_NOT_CONVERGED;
-            const double b = v[1] / rho_old;
+            const bool frozen = st->frozen;
+            if (frozen) status = -1;
+            const double b = frozen ? 0.0 : v[1] / rho_old;
             so.coef = (float)b;
             if (w0) {
                 st->err = err;
@@ -354,7 +356,7 @@ __device__ __noinline__ HeadOut head_b(const float2* __restrict__ pin, int nb_in
     __syncthreads();
     sum_partials<1>(pin, nb_in, v, reinterpret_cast<float2*>(sm));
     if (threadIdx.x == 0) {
-        const double rho = BOUT ? st->rho_next : st->rho, a = rho / v[0];
+        const double rho = BOUT ? st->rho_next : st->rho, a = st->frozen ? 0.0 : rho / v[0];
         so.coef = (float)a;
         if (blk == 0) {
             st->alpha = a;

@@ -423,6 +423,25 @@ les_status les_set_option(les_ctx* c, int option, int value)
     }
 }
 
+les_status les_get_option(const les_ctx* c, int option, int* value)
+{
+    if (!c || !value) return LES_BAD_ARG;
+    switch (option) {
+    case LES_OPT_GRAPH: *value = c->graph_on; return LES_OK;
+    case LES_OPT_PDL: *value = c->pdl; return LES_OK;
+    case LES_OPT_PHYS32: *value = c->phys32; return LES_OK;
+    case LES_OPT_TEST_STALL: *value = c->test_stall; return LES_OK;
+    case LES_OPT_COL_STRIDE: *value = c->col_stride; return LES_OK;
+    case LES_OPT_FUSED: *value = c->fused; return LES_OK;
+    case LES_OPT_TMA: *value = c->opt_tma; return LES_OK;
+    case LES_OPT_ROWS_A: *value = c->tune_tja; return LES_OK;
+    case LES_OPT_ROWS_B: *value = c->tune_tjb; return LES_OK;
+    case LES_OPT_CHUNK_A: *value = c->tune_cia; return LES_OK;
+    case LES_OPT_CHUNK_B: *value = c->tune_cib; return LES_OK;
+    default: return LES_BAD_ARG;
+    }
+}
+
 les_status les_mark(les_ctx* c, int mark)
 {
     if (!c || mark < 0 || mark >= 64) return LES_BAD_ARG;

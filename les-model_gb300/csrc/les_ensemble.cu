@@ -116,6 +116,7 @@ __global__ void k_round_begin(BatchCase* cs, int n)
             in->max_iter = C.inner_cap;
             in->k = 0;
             in->done = 0;
+            in->frozen = 0;
             in->iters = 0;
             in->status = LES_OK;
             in->beta = 0.0;

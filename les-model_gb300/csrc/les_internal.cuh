@@ -204,7 +204,9 @@ __device__ bool last_block_sum(double (&v)[NV], double* partials, unsigned* coun
 struct SolverState {
     double rho, alpha, beta, err, tol, pq, rr, rz, bnorm, maxdp;
     double scal[8];   // misc scalars (dt, lambda, ...)
-    int k, done, iters, max_iter, status, buf, pad0, pad1;
+    int k, done, iters, max_iter, status, buf;
+    int frozen;       // column passes under the autotuner: zero alpha and beta, no end
+    int pad1;
     double rho_next;  // the column passes' rho, handed from pass A to pass B
 };
 

@@ -140,6 +140,7 @@ __global__ void k_inner_init(SolverState* in, const SolverState* out, double inn
     in->max_iter = max_iter;
     in->k = 0;
     in->done = 0;
+    in->frozen = 0;
     in->iters = 0;
     in->status = LES_OK;
     in->beta = 0.0;

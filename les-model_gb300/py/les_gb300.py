@@ -343,6 +343,11 @@ class Context:
     def set_option(self, option, value):
         self._chk(self.lib.les_set_option(self.h, int(option), int(value)))
 
+    def get_option(self, option):
+        v = C.c_int()
+        self._chk(self.lib.les_get_option(self.h, int(option), C.byref(v)))
+        return v.value
+
     # --- accounting
     def mark(self, slot):
         self._chk(self.lib.les_mark(self.h, int(slot)))
