@@ -606,7 +606,8 @@ def run_ours(args):
     down = {k: host[k].data_ptr() for k in out_keys}
     hview = {k: host[k].numpy() for k in host}
 
-    rec = dict(ms=[], e2e_s=[], ms64=[], iters=[], outer=[], iters64=[], rres=[], rres64=[], err=[], errT=[])
+    rec = dict(ms=[], e2e_s=[], ms64=[], iters=[], outer=[], iters64=[], rres=[], rres64=[], err=[], errT=[],
+               phase=[])
     clocks = Clocks(dev)
     if pg:
         pg.barrier()
@@ -618,11 +619,15 @@ def run_ours(args):
         l2_flush()
         t0 = time.perf_counter()
         ctx.upload_many_ptr(up)
+        t1 = time.perf_counter()
         ctx.mark(0)
         st = ctx.step(prm)
         ctx.mark(1)
+        t2 = time.perf_counter()
         ctx.download_many_ptr(down)
-        rec["e2e_s"].append(time.perf_counter() - t0)
+        t3 = time.perf_counter()
+        rec["e2e_s"].append(t3 - t0)
+        rec["phase"].append((t1 - t0, t2 - t1, t3 - t2))
         rec["ms"].append(ctx.elapsed(0, 1))
         rec["iters"].append(st.iters)
         rec["outer"].append(st.outer)
@@ -670,6 +675,11 @@ def run_ours(args):
            "h2d_bytes_per_step": 8 * n * len(in_keys), "d2h_bytes_per_step": 8 * n * len(out_keys),
            "timing": "host wall clock of upload_many + les_step + download_many on the timed steps "
                      "(the same steps as value)"}
+    if rec["phase"]:   # where the end-to-end time goes, per step (host wall clock, means)
+        ph = np.mean(np.array(rec["phase"]), axis=0) * 1e3
+        e2e["ms_per_step"] = {"upload": float(ph[0]), "les_step": float(ph[1]), "download": float(ph[2])}
+        e2e["copy_gbs"] = {"h2d": e2e["h2d_bytes_per_step"] / ph[0] / 1e6,
+                           "d2h": e2e["d2h_bytes_per_step"] / ph[2] / 1e6}
 
     # ---- roofline of the dominant kernel (CUDA events during the profiled steps)
     peak, peak_kind = measured_peak()

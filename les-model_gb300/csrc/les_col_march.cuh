@@ -4,7 +4,7 @@
 // The row offsets of a strip are multiples of the row stride (nz cells).
 // With the stride a compile-time constant they become immediate offsets of
 // the loads and stores, which takes most of the address arithmetic out of
-// the marches (256x128x128 mixed step: 148.7 -> 170.3 Mcell-steps/s); the
+// the marches (256x128x128 mixed step: 148.7 -> 169.0 Mcell-steps/s); the
 // kernels are therefore compiled for the common strides 32, 64, 128 and 256,
 // one translation unit each (les_col_sjN.cu), and once for a stride read at
 // run time (SJF = 0, les_col.cu).  Every instance does the same arithmetic in

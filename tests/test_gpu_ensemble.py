@@ -100,13 +100,36 @@ def test_ensemble_autotune_keeps_the_solution():
 
 
 def test_autotune_single_context():
+    """The autotuner times whole inner iterations (pass A then pass B) and
+    leaves its choice in the strip-shape options, where les_get_option reads
+    it back: rows of pass A 8 or 16, of pass B 4 or 8 (Chebyshev degree 4),
+    chunk lengths within the grid; the step then converges with it."""
     spec = dict(shape=(96, 48, 64), h=1.0 / 32, box=(20, 32, 10, 22, 20, 32), cs=0.17, seed=3, noise=0.01)
     with G.Context(_mesh(spec)) as c:
         p = _params(spec, _setup(c, spec))
         us = c.autotune(p.pcg)
         assert 0 < us < 1e5
+        assert c.get_option(G.OPT_ROWS_A) in (8, 16) and c.get_option(G.OPT_ROWS_B) in (4, 8)
+        assert 1 <= c.get_option(G.OPT_CHUNK_A) <= 96 and 1 <= c.get_option(G.OPT_CHUNK_B) <= 96
         st = c.step(p)
         assert st.status == G.OK and st.residual < 1e-8 * st.b_norm
+
+
+def test_options_read_back():
+    """les_get_option returns each option's default, then the value set."""
+    spec = dict(shape=(24, 12, 12), h=1.0 / 32, box=(8, 12, 4, 8, 4, 8), cs=0.17, seed=1, noise=0.01)
+    with G.Context(_mesh(spec)) as c:
+        defaults = {G.OPT_FUSED: 1, G.OPT_TMA: 0, G.OPT_ROWS_A: 0, G.OPT_ROWS_B: 0, G.OPT_CHUNK_A: 0,
+                    G.OPT_CHUNK_B: 0, G.OPT_GRAPH: 1, G.OPT_PDL: 1, G.OPT_PHYS32: 1, G.OPT_TEST_STALL: 0,
+                    G.OPT_COL_STRIDE: 1}
+        for opt, v in defaults.items():
+            assert c.get_option(opt) == v, (opt, c.get_option(opt), v)
+        for opt, v in ((G.OPT_FUSED, 2), (G.OPT_ROWS_A, 16), (G.OPT_CHUNK_B, 12), (G.OPT_GRAPH, 0),
+                       (G.OPT_COL_STRIDE, 0)):
+            c.set_option(opt, v)
+            assert c.get_option(opt) == v
+        with pytest.raises(Exception):
+            c.get_option(99)
 
 
 @pytest.mark.parametrize("count,seed", [(6, 5), (3, 17)])
