@@ -411,6 +411,20 @@ les_status les_elapsed(les_ctx* ctx, int mark0, int mark1, double* ms);
 
 /* ---- one full time step, src/main.cpp:115-144 --------------------------- */
 les_status les_step(les_ctx* ctx, const les_step_params* prm, les_step_stats* stats);
+/* One step with host fields, for a host that keeps its fields in host memory
+ * (the drop-in use of src/main.cpp:108-165): the n_in host arrays are
+ * uploaded into their slots, the step runs, and the n_out slots are
+ * downloaded -- the result of les_upload_many + les_step +
+ * les_download_many, bit for bit.  With the PCG solver the downloads of
+ * LES_U_NEW/V_NEW/W_NEW, LES_NU_T and LES_P_RHS, final before the pressure
+ * solve, overlap it (from a second stream, released by an event after the
+ * step's physics); the rest follow the step.  Host arrays should be pinned.
+ * step_ms (optional): the step's own device time, CUDA events on the
+ * context's stream around it (not the copies).  Returns after the last
+ * download. */
+les_status les_step_io(les_ctx* ctx, const les_step_params* prm, les_step_stats* stats, int n_in,
+                       const int* in_slots, const double* const* in_hosts, int n_out, const int* out_slots,
+                       double* const* out_hosts, double* step_ms);
 
 #ifdef __cplusplus
 }

@@ -174,6 +174,8 @@ les_status les_create(const les_mesh* mesh, int device, les_ctx** out)
     TRY(cudaSetDevice(device), "cudaSetDevice");
     TRY(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device), "attr");
     TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    // recorded inside every captured step (les_step_io's early downloads wait on it)
+    TRY(cudaEventCreateWithFlags(&c->ev_pre, cudaEventDisableTiming), "cudaEventCreate");
     const size_t nb = sizeof(double) * (size_t)c->g.n;
     for (int s = 0; s < LES_NSLOTS; ++s) {
         TRY(cudaMalloc(&c->slot[s], nb), "cudaMalloc(field)");
@@ -227,6 +229,10 @@ void les_destroy(les_ctx* c)
     les::io_work_free(c->io);   // joins a file writer still running
     cudaFree(c->inlet);
     if (c->aux) cudaStreamDestroy(c->aux);
+    if (c->io_stream) cudaStreamDestroy(c->io_stream);
+    if (c->ev_pre) cudaEventDestroy(c->ev_pre);
+    for (auto& e : c->ev_io)
+        if (e) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }

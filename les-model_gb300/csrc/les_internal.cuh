@@ -333,6 +333,15 @@ struct les_ctx {
     int test_stall = 0;                   // LES_OPT_TEST_STALL
     int col_stride = 1;                   // LES_OPT_COL_STRIDE
     cudaStream_t aux = nullptr;           // capture stream for conditional-loop bodies
+    // les_step_io: an event recorded after the step's physics (before the
+    // pressure solve; an external event node of the captured step), the
+    // stream of the downloads it releases, and those downloads
+    cudaEvent_t ev_pre = nullptr;
+    cudaEvent_t ev_io[2] = {};            // the step's device time
+    cudaStream_t io_stream = nullptr;
+    int n_early = 0;
+    int early_slot[LES_NSLOTS] = {};
+    double* early_host[LES_NSLOTS] = {};
     struct les::StepGraph* sg[2] = {};
     int sg_last = 0;                      // slot of the graph launched last
     unsigned long long version = 0;       // bumped by every change a captured graph depends on

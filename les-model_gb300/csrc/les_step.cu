@@ -149,8 +149,27 @@ les_status les::emit_step(les_ctx* c, const les_step_params* prm)
 {
     les_status st;
     if ((st = emit_step_pre(c, prm, false))) return st;
+    // the fields final before the solve may leave now (les_step_io)
+    if (c->ev_pre && (st = check_cuda(c, cudaEventRecordWithFlags(c->ev_pre, c->stream, cudaEventRecordExternal),
+                                      "step event")))
+        return st;
     if ((st = capture_mixed_fused(c, &prm->pcg, view32_of(c), prm->rel_tol > 0 ? 1 : 0))) return st;
     return emit_step_post(c, prm);
+}
+
+// les_step_io's early downloads: after the event that follows the step's
+// physics, on the context's copy stream, from the slots as they are mapped
+// after the step (the velocity buffers swapped)
+static les_status early_downloads(les_ctx* c)
+{
+    if (!c->n_early) return LES_OK;
+    const size_t bytes = sizeof(double) * (size_t)c->g.n;
+    les_status st = check_cuda(c, cudaStreamWaitEvent(c->io_stream, c->ev_pre, 0), "early download wait");
+    for (int q = 0; q < c->n_early && !st; ++q)
+        st = check_cuda(c, cudaMemcpyAsync(c->early_host[q], c->slot[c->early_slot[q]], bytes, cudaMemcpyDeviceToHost,
+                                           c->io_stream),
+                        "early download");
+    return st;
 }
 
 static les_status step_graph(les_ctx* c, const les_step_params* prm, les_step_stats* stats)
@@ -200,6 +219,7 @@ static les_status step_graph(les_ctx* c, const les_step_params* prm, les_step_st
     if (st) return st;
     c->sg_last = g == c->sg[0] ? 0 : 1;
     if (!fresh) swap_velocity(c);   // the capture swapped the host pointers once; a replay must too
+    if ((st = early_downloads(c))) return st;
     if (!stats) {
         c->launches += g->captured;
         return LES_OK;
@@ -209,7 +229,74 @@ static les_status step_graph(les_ctx* c, const les_step_params* prm, les_step_st
     return LES_OK;
 }
 
+static les_status step_impl(les_ctx* c, const les_step_params* prm, les_step_stats* stats);
+
 extern "C" les_status les_step(les_ctx* c, const les_step_params* prm, les_step_stats* stats)
+{
+    if (!c || !prm) return LES_BAD_ARG;
+    c->n_early = 0;
+    return step_impl(c, prm, stats);
+}
+
+// Fields final when the pressure solve starts: nu_t, the solve's right-hand
+// side and the u_new buffers (after the momentum update's swap they hold the
+// step's incoming velocity, which nothing later writes)
+static bool final_before_solve(int slot)
+{
+    return slot == LES_U_NEW || slot == LES_V_NEW || slot == LES_W_NEW || slot == LES_NU_T || slot == LES_P_RHS;
+}
+
+extern "C" les_status les_step_io(les_ctx* c, const les_step_params* prm, les_step_stats* stats, int n_in,
+                                  const int* in_slots, const double* const* in_hosts, int n_out,
+                                  const int* out_slots, double* const* out_hosts, double* step_ms)
+{
+    if (!c || !prm || n_in < 0 || n_out < 0 || n_out > LES_NSLOTS || (n_out > 0 && (!out_slots || !out_hosts)))
+        return LES_BAD_ARG;
+    for (int q = 0; q < n_out; ++q)
+        if (out_slots[q] < 0 || out_slots[q] >= LES_NSLOTS || !out_hosts[q]) return LES_BAD_ARG;
+    cudaSetDevice(c->device);
+    les_status st = LES_OK;
+    for (int q = 0; q < 2 && !st; ++q)
+        if (!c->ev_io[q]) st = check_cuda(c, cudaEventCreate(&c->ev_io[q]), "step timing event");
+    if (!st && !c->io_stream)
+        st = check_cuda(c, cudaStreamCreateWithFlags(&c->io_stream, cudaStreamNonBlocking), "copy stream");
+    if (!st && n_in > 0) st = les_upload_many(c, n_in, in_slots, in_hosts);
+    if (st) return st;
+    // the downloads of fields final before the solve overlap it (PCG steps);
+    // the others follow the step
+    c->n_early = 0;
+    int late_slot[LES_NSLOTS];
+    double* late_host[LES_NSLOTS];
+    int n_late = 0;
+    for (int q = 0; q < n_out; ++q) {
+        if (prm->solver == LES_SOLVER_PCG && final_before_solve(out_slots[q])) {
+            c->early_slot[c->n_early] = out_slots[q];
+            c->early_host[c->n_early++] = out_hosts[q];
+        } else {
+            late_slot[n_late] = out_slots[q];
+            late_host[n_late++] = out_hosts[q];
+        }
+    }
+    st = check_cuda(c, cudaEventRecord(c->ev_io[0], c->stream), "step timing event");
+    if (!st) st = step_impl(c, prm, stats);
+    c->n_early = 0;
+    les_status st2 = check_cuda(c, cudaEventRecord(c->ev_io[1], c->stream), "step timing event");
+    const size_t bytes = sizeof(double) * (size_t)c->g.n;
+    for (int q = 0; q < n_late && !st && !st2; ++q)
+        st2 = check_cuda(c, cudaMemcpyAsync(late_host[q], c->slot[late_slot[q]], bytes, cudaMemcpyDeviceToHost,
+                                            c->stream),
+                         "field download");
+    les_status s1 = check_cuda(c, cudaStreamSynchronize(c->io_stream), "copy stream sync");
+    les_status s2 = check_cuda(c, cudaStreamSynchronize(c->stream), "step sync");
+    if (!st && !st2 && !s1 && !s2 && step_ms) {
+        float ms = 0.f;
+        st2 = check_cuda(c, cudaEventElapsedTime(&ms, c->ev_io[0], c->ev_io[1]), "step time");
+        *step_ms = ms;
+    }
+    return st ? st : (st2 ? st2 : (s1 ? s1 : s2));
+}
+
+static les_status step_impl(les_ctx* c, const les_step_params* prm, les_step_stats* stats)
 {
     if (!c || !prm) return LES_BAD_ARG;
     if (prm->solver < LES_SOLVER_PCG || prm->solver > LES_SOLVER_GS_SOR) return LES_BAD_ARG;
@@ -233,6 +320,10 @@ extern "C" les_status les_step(les_ctx* c, const les_step_params* prm, les_step_
     s.dt = dt;
     if (prm->solver == LES_SOLVER_PCG) {
         if ((st = div_b_dev(c, dt, prm->rho, prm->rel_tol, nullptr))) return st;
+        if (c->n_early) {
+            if ((st = check_cuda(c, cudaEventRecord(c->ev_pre, c->stream), "step event"))) return st;
+            if ((st = early_downloads(c))) return st;
+        }
         les_pcg_result r{};
         const int keep = prm->rel_tol > 0 ? 1 : 0;
         if (prm->pcg.precision == LES_MIXED) solve = pcg_mixed_impl(c, &prm->pcg, &r, keep);

@@ -340,6 +340,20 @@ class Context:
         self._chk(self.lib.les_step(self.h, C.byref(params), C.byref(s)))
         return s
 
+    def step_io(self, params, up, down):
+        """One step with host fields: {slot: host pointer} uploaded before it,
+        {slot: host pointer} downloaded after it (les_step_io); returns
+        (stats, device ms of the step)."""
+        s = StepStats()
+        ms = C.c_double()
+        ni, no = len(up), len(down)
+        si = (C.c_int * max(ni, 1))(*[SLOTS.get(k, k) for k in up])
+        pi = (_dp * max(ni, 1))(*[C.cast(p, _dp) for p in up.values()])
+        so = (C.c_int * max(no, 1))(*[SLOTS.get(k, k) for k in down])
+        po = (_dp * max(no, 1))(*[C.cast(p, _dp) for p in down.values()])
+        self._chk(self.lib.les_step_io(self.h, C.byref(params), C.byref(s), ni, si, pi, no, so, po, C.byref(ms)))
+        return s, ms.value
+
     def set_option(self, option, value):
         self._chk(self.lib.les_set_option(self.h, int(option), int(value)))
 

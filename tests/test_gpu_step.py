@@ -259,6 +259,64 @@ def test_graph_step_matches_launch_by_launch(shape, fused, dt_fixed):
         assert same(f0[k], f1[k]), k
 
 
+IO_IN = ("u", "v", "w", "u_new", "v_new", "w_new", "p", "nu_t")
+IO_OUT = ("u", "v", "w", "u_new", "v_new", "w_new", "p", "p_rhs", "nu_t")
+
+
+@pytest.mark.parametrize("graph,precision", [(1, G.MIXED), (0, G.MIXED), (0, G.FP64)],
+                         ids=["graph-mixed", "launches-mixed", "launches-fp64"])
+def test_step_io_matches_separate_calls(graph, precision):
+    """les_step_io (upload, step, download in one call; the downloads of
+    u_new, v_new, w_new, nu_t and p_rhs overlap the pressure solve, released
+    by an event after the step's physics) gives what les_upload_many +
+    les_step + les_download_many give, bit for bit, every step -- the host's
+    fields fed back into the next step as a drop-in host loop does."""
+    shape = (64, 32, 32)
+    n = int(np.prod(shape))
+    solid = les_cases.box_mask(shape, (16, 20, 10, 14, 10, 14))
+    f = les_cases.init_fields(shape, 0.01, 77)
+    h = 1.0 / 32
+    m = G.Mesh(*shape, h, h, h)
+    with G.Context(m) as c:
+        c.upload_mask(np.zeros(n, np.uint8))
+        c.build_stencil()
+        lmax = c.lambda_max(20)
+    prm = G.step_params(nu=les_cases.NU, rho=les_cases.RHO, cs=les_cases.CS, cfl_conv=les_cases.CFL_CONV,
+                        solver=G.SOLVER_PCG, rel_tol=1e-8,
+                        pcg=G.pcg_opts(precond=G.PC_CHEBYSHEV, max_iter=5000, lambda_min=3 * np.pi ** 2,
+                                       lambda_max=lmax, degree=4, precision=precision, inner_rtol=1e-4))
+    host = [{k: np.zeros(n) for k in IO_OUT} for _ in range(2)]
+    ctxs = []
+    try:
+        for hb in host:
+            c = G.Context(m)
+            ctxs.append(c)
+            c.set_option(G.OPT_GRAPH, graph)
+            c.upload_mask(np.zeros(n, np.uint8))
+            c.build_stencil()
+            c.upload_fields(f)
+            c.upload_mask(solid)
+            c.velocity_bcs()
+            for k in IO_OUT:
+                hb[k][:] = c.download(k)
+        for step in range(5):
+            a, b = ctxs
+            ha, hb = host
+            a.upload_many_ptr({k: ha[k].ctypes.data for k in IO_IN})
+            sa = a.step(prm)
+            for k in IO_OUT:
+                a.download_ptr(k, ha[k].ctypes.data)
+            sb, ms = b.step_io(prm, {k: hb[k].ctypes.data for k in IO_IN}, {k: hb[k].ctypes.data for k in IO_OUT})
+            assert ms > 0
+            assert (sa.dt, sa.iters, sa.outer, sa.residual, sa.status) == (sb.dt, sb.iters, sb.outer, sb.residual,
+                                                                          sb.status), step
+            for k in IO_OUT:
+                assert same(ha[k], hb[k]), (step, k)
+    finally:
+        for c in ctxs:
+            c.close()
+
+
 @pytest.mark.parametrize("graph", [0, 1], ids=["launches", "graph"])
 def test_dependent_launch_changes_nothing(graph):
     """The column passes as programmatic dependent launches (each waits for
