@@ -349,7 +349,8 @@ def run_batch(args):
                                                 inner_rtol=args.inner_rtol)))
     cells = sum(int(np.prod(s["shape"])) for s in specs)
     t0 = time.perf_counter()
-    tune_us = ens.autotune(prm[0].pcg) if args.tune and not args.ens_batched else None
+    tune_us = ens.autotune(prm[0].pcg) if args.tune else None   # batched: the work split; else per case
+    split = ens.batch_split()
     tune_s = time.perf_counter() - t0
     t0 = time.perf_counter()
     for _ in range(args.warmup):
@@ -392,8 +393,10 @@ def run_batch(args):
                        "l2": "inputs (~%.1f GB) larger than L2" % (cells * 120 / 1e9),
                        "pdl": 0 if args.pdl is None else args.pdl, "phys32": args.phys32,
                        "form": "batched solves" if args.ens_batched else "one branch per case",
-                       "split": ("static: whole-length strips, then one more chunk for the longest march until "
-                                 "the items reach 4x the resident warps" if args.ens_batched else
+                       "split": ("whole-length strips, then one more chunk for the longest march until the "
+                                 "items reach %dx the resident warps (%s)" %
+                                 (split, "chosen by the ensemble autotuner from 2, 3, 4, 6"
+                                  if args.tune else "the default") if args.ens_batched else
                                  "per case from the ensemble autotuner"),
                        "autotune_us_per_iteration": tune_us, "autotune_s": tune_s,
                        "first_steps_with_capture_s": warm_s},

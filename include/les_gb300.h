@@ -337,6 +337,12 @@ les_status les_autotune(les_ctx* ctx, const les_pcg_opts* opts, double share, do
  * candidate concurrently, as in a step), choosing one setting per case
  * from the total time. */
 les_status les_ensemble_autotune(les_ensemble* ens, const les_pcg_opts* opts, double* best_us);
+/* In the batched form (les_ensemble_set_batched, default) les_ensemble_autotune
+ * chooses instead how finely the batched passes split the cases' marches:
+ * items up to `split` times the GPU's resident warps (2, 3, 4 or 6; 4 before
+ * tuning), timed as batched inner iterations over all cases; best_us is then
+ * the time of one such iteration.  This returns the split in use. */
+int les_ensemble_batch_split(const les_ensemble* ens);
 /* 1 (default): the cases' mixed-precision solves run batched -- every inner
  * pass, defect and update is one kernel over all cases, and the solver loops
  * run while any case iterates (used when all cases run the register-column

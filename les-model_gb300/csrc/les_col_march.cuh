@@ -508,7 +508,7 @@ __device__ __forceinline__ void col_a(const Geo& g, const ColMap& m, const Coef&
     if (last_block_sum_df<1>(va, reinterpret_cast<float2*>(partials), counter, reinterpret_cast<float2*>(sm), blk,
                              nblk, v)) {
         if (threadIdx.x == 0) {
-            st->alpha = st->rho / v[0];
+            st->alpha = st->frozen ? 0.0 : st->rho / v[0];
             st->buf = pslot;   // buffer holding this iteration's p
         }
     }
@@ -547,6 +547,7 @@ __device__ __forceinline__ void pass_b_finish(const Acc& arr, const Acc& arz, do
                 st->err = err;
                 const int total = outer->iters + 1;
                 outer->iters = total;
+                if (st->frozen) { st->beta = 0.0; return; }   // the autotuner's timing rounds
                 if (err < st->tol) { st->done = 1; st->status = LES_OK; }
                 else if (!isfinite(err)) { st->done = 1; st->status = LES_NONFINITE; }
                 else if (kk >= st->max_iter || total >= total_cap) { st->done = 1; st->status = LES_NOT_CONVERGED; }

@@ -38,6 +38,7 @@ struct les_ensemble {
     cudaStream_t main = nullptr;
     cudaEvent_t ev = nullptr;       // fork / join / ordering
     int batched = 1;                // les_ensemble_set_batched
+    int split = 4;                  // batched passes: items per pass up to split x the resident warps
     unsigned long long* d_count = nullptr;   // batched kernels run (added by the loop conditions)
     struct Graph {
         std::vector<les_step_params> prm;
@@ -46,6 +47,7 @@ struct les_ensemble {
         std::vector<unsigned long long> version, captured;
         cudaGraphExec_t exec = nullptr;
         int req = -1;                         // e->batched when captured
+        int split = 0;                        // e->split when captured
         bool batched = false;                 // the form captured (branches if the cases cannot batch)
         les::BatchCase* d_cases = nullptr;    // batched form: case table, grid order
         int* d_pre = nullptr;                 // block starts: A, B, defect, update (4 x (n + 1))
@@ -79,7 +81,7 @@ void graph_clear(les_ensemble::Graph& g)
 
 bool graph_matches(const les_ensemble* e, const les_ensemble::Graph& g, const les_step_params* prm)
 {
-    if (!g.exec || g.req != e->batched) return false;
+    if (!g.exec || g.req != e->batched || g.split != e->split) return false;
     for (size_t i = 0; i < e->cs.size(); ++i) {
         const les_ctx* c = e->cs[i];
         if (g.version[i] != c->version || g.tau[i] != c->tau ||
@@ -92,7 +94,7 @@ bool graph_matches(const les_ensemble* e, const les_ensemble::Graph& g, const le
 
 bool same_params(const les_ensemble* e, const les_ensemble::Graph& g, const les_step_params* prm)
 {
-    if (!g.exec || g.req != e->batched) return false;
+    if (!g.exec || g.req != e->batched || g.split != e->split) return false;
     for (size_t i = 0; i < e->cs.size(); ++i)
         if (g.version[i] != e->cs[i]->version || std::memcmp(&g.prm[i], &prm[i], sizeof(les_step_params)) != 0)
             return false;
@@ -180,10 +182,12 @@ bool batchable(les_ensemble* e, const les_step_params* prm)
 
 // Work splits of the batched column passes: each case starts with one chunk
 // per strip (whole-length marches); while all cases' items are fewer than
-// four times the GPU's resident warps, the case with the longest march gets
-// one chunk more.  Many short, similar items let the block scheduler balance
-// the ragged cases (64-case batch, GB300: 1x resident 162, 2x 194, 3x 207,
-// 4x 210, 6x 203 Mcell-steps/s).  Grid order: longest marches first.
+// e->split times the GPU's resident warps, the case with the longest march
+// gets one chunk more.  Many short, similar items let the block scheduler
+// balance the ragged cases (64-case batch, GB300: 1x resident 162, 2x 194,
+// 3x 207, 4x 210, 6x 203 Mcell-steps/s); the default is 4 and
+// les_ensemble_autotune times 2, 3, 4 and 6.  Grid order: longest marches
+// first.
 les_status batch_plan(les_ensemble* e, const les_step_params* prm, les_ensemble::Graph& g, BatchLayout& L)
 {
     const int n = (int)e->cs.size();
@@ -201,7 +205,7 @@ les_status batch_plan(les_ensemble* e, const les_step_params* prm, les_ensemble:
             total += m[i].items;
         }
         const int min_ci = 2 * halo > 4 ? 2 * halo : 4;
-        while (total < 4LL * resident) {
+        while (total < (long long)e->split * resident) {
             int best = -1;
             for (int i = 0; i < n; ++i)
                 if (m[i].ci / 2 >= min_ci && (best < 0 || m[i].ci > m[best].ci)) best = i;
@@ -443,11 +447,80 @@ les_status capture_branches(les_ensemble* e, const les_step_params* prm, les_ens
 les_status capture(les_ensemble* e, const les_step_params* prm, les_ensemble::Graph& g)
 {
     les_status st = (e->batched && batchable(e, prm)) ? capture_batched(e, prm, g) : capture_branches(e, prm, g);
-    if (!st) g.req = e->batched;
+    if (!st) {
+        g.req = e->batched;
+        g.split = e->split;
+    }
     return st;
 }
 
 }  // namespace
+
+// les_ensemble_autotune's batched form: for each candidate work split, the
+// case table of the batched plan and KT timing rounds of the batched passes
+// A and B over all cases (inputs and frozen states of the single-case
+// tuner); keeps the fastest split.
+les_status les::ensemble_tune_batched(les_ensemble* e, const les_pcg_opts* o, double* best_us, int* handled)
+{
+    *handled = 0;
+    const int n = (int)e->cs.size();
+    std::vector<les_step_params> prm(n);
+    for (auto& p : prm) {
+        p = les_step_params{};
+        p.solver = LES_SOLVER_PCG;
+        p.pcg = *o;
+        p.pcg.precision = LES_MIXED;
+    }
+    if (!e->batched || !batchable(e, prm.data())) return LES_OK;
+    *handled = 1;
+    cudaSetDevice(e->device);
+    les_status st = ecuda(e, cudaStreamSynchronize(e->main), "tune sync");
+    for (int i = 0; i < n && !st; ++i) {
+        les_ctx* c = e->cs[i];
+        st = tune_prep(c);
+        if (!st) st = ecuda(e, cudaStreamSynchronize(c->stream), "tune prep");
+        if (st == LES_CUDA_ERROR || st == LES_BAD_ARG) st = efail(e, st, "case " + std::to_string(i) + ": " + c->err);
+    }
+    if (st) return st;
+    constexpr int KT = 6;
+    const int cand[4] = {2, 3, 4, 6};
+    const int saved = e->split;
+    double best = 1e30;
+    int pick = saved;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    st = ecuda(e, cudaEventCreate(&e0), "tune event");
+    if (!st) st = ecuda(e, cudaEventCreate(&e1), "tune event");
+    for (int q = 0; q < 4 && !st; ++q) {
+        e->split = cand[q];
+        les_ensemble::Graph tg;   // the case table and block starts only
+        BatchLayout L;
+        st = batch_plan(e, prm.data(), tg, L);
+        const int* pa = tg.d_pre;
+        const int* pb = tg.d_pre + (n + 1);
+        for (int rep = 0; rep < 2 && !st; ++rep) {   // rep 0 warms up
+            st = ecuda(e, cudaEventRecord(e0, e->main), "tune event");
+            for (int k = 0; k < KT && !st; ++k) {
+                st = col_batch_pass_a(e->main, false, k & 1, tg.d_cases, pa, n, L.blocks[0]);
+                if (!st) st = col_batch_pass_b(e->main, L.S, false, k & 1, tg.d_cases, pb, n, L.blocks[1]);
+                if (st) st = ecuda(e, cudaGetLastError(), "tune pass");
+            }
+            if (!st) st = ecuda(e, cudaEventRecord(e1, e->main), "tune event");
+        }
+        float ms = 0.f;
+        if (!st) st = ecuda(e, cudaEventSynchronize(e1), "tune timing");
+        if (!st) st = ecuda(e, cudaEventElapsedTime(&ms, e0, e1), "tune timing");
+        graph_clear(tg);
+        if (!st && 1e3 * ms / KT < best) {
+            best = 1e3 * ms / KT;
+            pick = cand[q];
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    e->split = st ? saved : pick;
+    if (!st && best_us) *best_us = best;
+    return st;
+}
 
 extern "C" {
 
@@ -565,6 +638,8 @@ les_status les_ensemble_step(les_ensemble* e, const les_step_params* prm, les_st
     }
     return LES_OK;
 }
+
+int les_ensemble_batch_split(const les_ensemble* e) { return e ? e->split : 0; }
 
 les_status les_ensemble_set_batched(les_ensemble* e, int on)
 {

@@ -206,6 +206,10 @@ __device__ __forceinline__ int batch_case(const int* pre, int n, int block)
 
 // column passes over all cases (S levels; rows as in the single-case default)
 int col_batch_tj_b(int S);
+les_status tune_prep(les_ctx* c);   // the autotuner's inputs and frozen state (les_tune.cu)
+// les_ensemble_autotune for a batched ensemble: times its work splits
+// (*handled = 0 when the ensemble does not run batched)
+les_status ensemble_tune_batched(les_ensemble* e, const les_pcg_opts* o, double* best_us, int* handled);
 int col_batch_warps_per_block();   // warps of a batched column-pass block (one item each)
 ColMap col_batch_map(les_ctx* c, int pass, int S, int chunk_planes);   // pass 0: A, 1: B
 int col_batch_resident_warps(int pass, int S);

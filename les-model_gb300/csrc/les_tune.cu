@@ -211,6 +211,11 @@ les_status tune(std::vector<Case>& cs, cudaStream_t main, double base, double* b
 
 }  // namespace
 
+namespace les {
+// The inputs and frozen solver state of the autotuner's timing rounds
+les_status tune_prep(les_ctx* c) { return prep(c); }
+}  // namespace les
+
 extern "C" {
 
 les_status les_autotune(les_ctx* c, const les_pcg_opts* o, double share, double* best_us)
@@ -231,6 +236,9 @@ les_status les_ensemble_autotune(les_ensemble* e, const les_pcg_opts* o, double*
 {
     const int n = les_ensemble_size(e);
     if (!e || !o || n < 1) return LES_BAD_ARG;
+    int handled = 0;   // the batched form tunes its work split
+    les_status bst = les::ensemble_tune_batched(e, o, best_us, &handled);
+    if (handled || bst) return bst;
     std::vector<Case> cs(n);
     for (int i = 0; i < n; ++i) {
         les_ctx* c = les_ensemble_case(e, i);

@@ -473,6 +473,10 @@ class Ensemble:
         cases); 0: one graph branch per case."""
         self._chk(self.lib.les_ensemble_set_batched(self.h, int(on)))
 
+    def batch_split(self):
+        """Items of a batched pass, in multiples of the resident warps."""
+        return self.lib.les_ensemble_batch_split(self.h)
+
     def close(self):
         if self.h:
             for c in self.cases:

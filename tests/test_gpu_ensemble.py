@@ -81,12 +81,20 @@ def test_ensemble_matches_cases_stepped_alone():
             assert same(f[key], efields[i][key]), (i, key)
 
 
-def test_ensemble_autotune_keeps_the_solution():
+@pytest.mark.parametrize("batched", [1, 0], ids=["batched", "branches"])
+def test_ensemble_autotune_keeps_the_solution(batched):
+    """The ensemble autotuner -- the batched form's work split (timed
+    batched iterations over all cases, frozen states), or each case's strip
+    shape for the branch form -- changes how the work is cut, not the
+    solution; the step after it starts from a fresh solver state."""
     specs = _specs(4, 23)
     with G.Ensemble([_mesh(s) for s in specs]) as ens:
+        ens.set_batched(batched)
         prm = [_params(s, _setup(c, s)) for c, s in zip(ens.cases, specs)]
         us = ens.autotune(prm[0].pcg)
         assert us > 0
+        if batched:
+            assert ens.batch_split() in (2, 3, 4, 6)
         stats = ens.step(prm)
         tuned = [c.download("p") for c in ens.cases]
     for i, s in enumerate(specs):
