@@ -151,12 +151,13 @@ __global__ void k_spmv(Geo g, StencilView A, const double* __restrict__ p, doubl
     if (dot_mode == DOT_ALPHA && st->done) return;
     int i, j, k;
     double pq[1] = {0.0};
-    if (cell_coords(g, i, j, k)) {
-        const int id = i * g.si + j * g.sj + k;
-        double val = apply_row(A, p, g, i, j, k, id);
-        q[id] = val;
-        pq[0] = p[id] * val;
-    }
+    if (cell_coords(g, i, j, k))
+        for (; i < g.nx; i += gridDim.z) {   // planes blockIdx.z, + gridDim.z, ...
+            const int id = i * g.si + j * g.sj + k;
+            double val = apply_row(A, p, g, i, j, k, id);
+            q[id] = val;
+            pq[0] += p[id] * val;
+        }
     if (dot_mode == DOT_NONE) return;
     if (last_block_sum<1>(pq, partials, counter, sm)) {
         if (threadIdx.x == 0 && threadIdx.y == 0) {
@@ -208,18 +209,19 @@ __global__ void k_update(Geo g, StencilView A, double* __restrict__ x, double* _
     const double alpha = st->alpha;
     int i, j, k;
     double acc[2] = {0.0, 0.0};
-    if (cell_coords(g, i, j, k)) {
-        const int id = i * g.si + j * g.sj + k;
-        x[id] += alpha * p[id];
-        double rv = r[id] + (-alpha) * q[id];
-        r[id] = rv;
-        acc[0] = rv * rv;
-        if (jacobi) {
-            double zv = rv / A.diag(id);
-            z[id] = zv;
-            acc[1] = rv * zv;
+    if (cell_coords(g, i, j, k))
+        for (; i < g.nx; i += gridDim.z) {   // planes blockIdx.z, + gridDim.z, ...
+            const int id = i * g.si + j * g.sj + k;
+            x[id] += alpha * p[id];
+            double rv = r[id] + (-alpha) * q[id];
+            r[id] = rv;
+            acc[0] += rv * rv;
+            if (jacobi) {
+                double zv = rv / A.diag(id);
+                z[id] = zv;
+                acc[1] += rv * zv;
+            }
         }
-    }
     if (last_block_sum<2>(acc, partials, counter, sm)) {
         if (threadIdx.x == 0 && threadIdx.y == 0) {
             double e = sqrt(acc[0]);
@@ -250,10 +252,11 @@ __global__ void k_dot(Geo g, const double* __restrict__ a, const double* __restr
     if (skip_done && st->done) return;
     int i, j, k;
     double s[1] = {0.0};
-    if (cell_coords(g, i, j, k)) {
-        const int id = i * g.si + j * g.sj + k;
-        s[0] = a[id] * b[id];
-    }
+    if (cell_coords(g, i, j, k))
+        for (; i < g.nx; i += gridDim.z) {   // planes blockIdx.z, + gridDim.z, ...
+            const int id = i * g.si + j * g.sj + k;
+            s[0] += a[id] * b[id];
+        }
     if (last_block_sum<1>(s, partials, counter, sm)) {
         if (threadIdx.x == 0 && threadIdx.y == 0) {
             if (mode == RD_RHO) st->rho = s[0];
@@ -598,6 +601,20 @@ les_status ensure_stored_A(les_ctx* c)
     return check_launch(c, "expand stencil");
 }
 
+// Grid of the FP64 solver's reductions in its iterations: every (k, j) tile
+// once and the i-planes shared out so that about eight blocks per SM run,
+// each summing its planes before the grid sum -- one partial, fence and
+// atomic per block instead of one per block and plane (16384 at
+// 256x128x128).  The kernels loop over planes i = blockIdx.z + t gridDim.z.
+static dim3 reduce_grid(const les_ctx* c)
+{
+    dim3 gr = cell_grid(c->g);
+    const long long tiles = (long long)gr.x * gr.y;
+    const long long z = (8LL * c->sms + tiles - 1) / tiles;
+    gr.z = (unsigned)(z < 1 ? 1 : (z > c->g.nx ? c->g.nx : z));
+    return gr;
+}
+
 // PCG of src/pressure.cpp:342-414 in FP64 with the solution in P and the
 // right-hand side in B.  The loop runs on the device; the host only polls
 // the state between batches of iterations (kernels after convergence exit
@@ -631,16 +648,17 @@ les_status pcg_fp64(les_ctx* c, const les_pcg_opts* o, les_pcg_result* res, int 
         return c->h_state->done ? (les_status)c->h_state->status : LES_NOT_CONVERGED;
     }
     const bool jac = o->precond == LES_PC_JACOBI;
+    const dim3 grr = reduce_grid(c);
     int launched = 0, batch = 4;
     for (;;) {
         for (int it = 0; it < batch; ++it) {
-            launch_p(c, PROF_SPMV64, k_spmv, gr, bl, g, A, p, q, c->partials, c->counters + 1, c->state, DOT_ALPHA);
-            launch_p(c, PROF_UPDATE64, k_update, gr, bl, g, A, x, r, p, q, z, c->partials, c->counters + 5, c->state,
+            launch_p(c, PROF_SPMV64, k_spmv, grr, bl, g, A, p, q, c->partials, c->counters + 1, c->state, DOT_ALPHA);
+            launch_p(c, PROF_UPDATE64, k_update, grr, bl, g, A, x, r, p, q, z, c->partials, c->counters + 5, c->state,
                                                 jac ? 1 : 0);
             if (!jac) {
                 st = precond_dev(c, o, r, z, 1);
                 if (st) return st;
-                launch(c, k_dot, gr, bl, g, r, z, c->partials, c->counters + 2, c->state, RD_BETA, 1);
+                launch(c, k_dot, grr, bl, g, r, z, c->partials, c->counters + 2, c->state, RD_BETA, 1);
             }
             launch(c, k_pupdate, gr, bl, g, z, p, c->state);
         }
