@@ -260,8 +260,18 @@ extern "C" les_status les_step_io(les_ctx* c, const les_step_params* prm, les_st
         if (!c->ev_io[q]) st = check_cuda(c, cudaEventCreate(&c->ev_io[q]), "step timing event");
     if (!st && !c->io_stream)
         st = check_cuda(c, cudaStreamCreateWithFlags(&c->io_stream, cudaStreamNonBlocking), "copy stream");
-    if (!st && n_in > 0) st = les_upload_many(c, n_in, in_slots, in_hosts);
-    if (st) return st;
+    // the uploads precede the step in the context's stream: no host wait
+    if (!st && n_in > 0 && (!in_slots || !in_hosts)) st = LES_BAD_ARG;
+    for (int q = 0; q < n_in && !st; ++q)
+        if (in_slots[q] < 0 || in_slots[q] >= LES_NSLOTS || !in_hosts[q]) st = LES_BAD_ARG;
+    const size_t bytes = sizeof(double) * (size_t)c->g.n;
+    for (int q = 0; q < n_in && !st; ++q)
+        st = check_cuda(c, cudaMemcpyAsync(c->slot[in_slots[q]], in_hosts[q], bytes, cudaMemcpyHostToDevice, c->stream),
+                        "field upload");
+    if (st) {
+        cudaStreamSynchronize(c->stream);
+        return st;
+    }
     // the downloads of fields final before the solve overlap it (PCG steps);
     // the others follow the step
     c->n_early = 0;
@@ -281,7 +291,6 @@ extern "C" les_status les_step_io(les_ctx* c, const les_step_params* prm, les_st
     if (!st) st = step_impl(c, prm, stats);
     c->n_early = 0;
     les_status st2 = check_cuda(c, cudaEventRecord(c->ev_io[1], c->stream), "step timing event");
-    const size_t bytes = sizeof(double) * (size_t)c->g.n;
     for (int q = 0; q < n_late && !st && !st2; ++q)
         st2 = check_cuda(c, cudaMemcpyAsync(late_host[q], c->slot[late_slot[q]], bytes, cudaMemcpyDeviceToHost,
                                             c->stream),
