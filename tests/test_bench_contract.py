@@ -16,9 +16,10 @@ def test_reference_arm_line():
     assert p.returncode == 0, p.stderr[-2000:]
     line = [l for l in p.stdout.splitlines() if l.startswith("{")][-1]
     d = json.loads(line)
-    base = json.load(open(os.path.join(ROOT, "BASELINE.json")))
+    sys.path.insert(0, ROOT)
+    import bench
     assert d["impl"] == "reference"
-    assert d["metric"] == base["metric"]
+    assert d["metric"] == bench.METRIC   # the same metric line as the GPU arm
     assert d["unit"] == "Mcell-steps/s" and d["higher_is_better"] is True
     assert d["steps"] == 1 and d["warmup"] == 0 and d["n_gpus"] == 1
     assert d["value"] > 0 and d["ms_per_step"] > 0

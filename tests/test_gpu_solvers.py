@@ -309,7 +309,7 @@ def test_compiled_row_strides_match_runtime_stride(shape, pc, deg, rows):
 
 @pytest.mark.parametrize("cap", [1, 2, 7])
 def test_mixed_column_solve_stops_at_the_iteration_cap(cap):
-    """The register-column passes judge an inner iteration in the pass after
+    """The register-column passes test an inner iteration in the pass after
     it (each pass's grid sums are formed by the next one): a mixed solve
     capped at `cap` inner iterations must still stop after exactly `cap` of
     them, report NOT_CONVERGED and leave a finite solution."""
