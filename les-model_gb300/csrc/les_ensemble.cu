@@ -297,11 +297,10 @@ les_status emit_batched_solve(les_ensemble* e, les_ensemble::Graph& g, const Bat
                     return launched("inner condition");
                 },
                 [&](cudaGraphConditionalHandle hi) -> les_status {
-                    les_status s3;
-                    if ((s3 = col_batch_pass_a(s, false, 1, cs, pa, n, L.blocks[0]))) return launched("batched pass A");
-                    if ((s3 = col_batch_pass_b(s, L.S, false, 0, cs, pb, n, L.blocks[1]))) return launched("batched pass B");
-                    if ((s3 = col_batch_pass_a(s, false, 0, cs, pa, n, L.blocks[0]))) return launched("batched pass A");
-                    if ((s3 = col_batch_pass_b(s, L.S, false, 1, cs, pb, n, L.blocks[1]))) return launched("batched pass B");
+                    if (col_batch_pass_a(s, false, 1, cs, pa, n, L.blocks[0])) return launched("batched pass A");
+                    if (col_batch_pass_b(s, L.S, false, 0, cs, pb, n, L.blocks[1])) return launched("batched pass B");
+                    if (col_batch_pass_a(s, false, 0, cs, pa, n, L.blocks[0])) return launched("batched pass A");
+                    if (col_batch_pass_b(s, L.S, false, 1, cs, pb, n, L.blocks[1])) return launched("batched pass B");
                     k_cond_any_inner<<<1, 256, 0, s>>>(cs, n, hi, cnt, 5);
                     return launched("inner condition");
                 });
