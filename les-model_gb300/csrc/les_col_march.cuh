@@ -51,12 +51,13 @@ namespace {
 
 // Block shapes.  A pass's deferred head sums every block partial of the
 // pass before it, so fewer, larger blocks make the head cheaper: a
-// single-case kernel that fits an even number of 4-warp blocks on an SM runs
-// half as many 8-warp blocks instead (256x128x128: 146.3 Mcell-steps/s with
-// 4-warp blocks, 149.1 with 8; 512x256x256: 107.9 and 107.2).  The batched
+// single-case kernel that fits 4-warp blocks on an SM in a multiple of four
+// runs 16-warp blocks, in a multiple of two 8-warp blocks (256x128x128:
+// 146.3 Mcell-steps/s with 4-warp blocks, 149.1 with 8; pass A in 16-warp
+// blocks: 167.7 -> 168.5; 512x256x256 unchanged within 0.7 %).  The batched
 // kernels sum their partials in a separate kernel and keep 4 warps.
-constexpr int col_threads(int blocks4) { return blocks4 % 2 == 0 ? 256 : 128; }
-constexpr int col_blocks(int blocks4) { return blocks4 % 2 == 0 ? blocks4 / 2 : blocks4; }
+constexpr int col_threads(int blocks4) { return blocks4 % 4 == 0 ? 512 : (blocks4 % 2 == 0 ? 256 : 128); }
+constexpr int col_blocks(int blocks4) { return blocks4 % 4 == 0 ? blocks4 / 4 : (blocks4 % 2 == 0 ? blocks4 / 2 : blocks4); }
 constexpr int blocks4_a(int TJ) { return TJ == 8 ? 4 : 2; }               // 4-warp blocks per SM
 constexpr int blocks4_b(int S, int TJ) { return (TJ == 4 && S <= 3) ? 3 : 2; }
 constexpr int CTB = 128;          // batched kernels: threads per block
