@@ -252,6 +252,7 @@ extern "C" les_status les_step_io(les_ctx* c, const les_step_params* prm, les_st
 {
     if (!c || !prm || n_in < 0 || n_out < 0 || n_out > LES_NSLOTS || (n_out > 0 && (!out_slots || !out_hosts)))
         return LES_BAD_ARG;
+    if (prm->solver < LES_SOLVER_PCG || prm->solver > LES_SOLVER_GS_SOR) return LES_BAD_ARG;   // before any copy
     for (int q = 0; q < n_out; ++q)
         if (out_slots[q] < 0 || out_slots[q] >= LES_NSLOTS || !out_hosts[q]) return LES_BAD_ARG;
     cudaSetDevice(c->device);
@@ -261,9 +262,9 @@ extern "C" les_status les_step_io(les_ctx* c, const les_step_params* prm, les_st
     if (!st && !c->io_stream)
         st = check_cuda(c, cudaStreamCreateWithFlags(&c->io_stream, cudaStreamNonBlocking), "copy stream");
     // the uploads precede the step in the context's stream: no host wait
-    if (!st && n_in > 0 && (!in_slots || !in_hosts)) st = LES_BAD_ARG;
+    if (!st && n_in > 0 && (!in_slots || !in_hosts)) return LES_BAD_ARG;
     for (int q = 0; q < n_in && !st; ++q)
-        if (in_slots[q] < 0 || in_slots[q] >= LES_NSLOTS || !in_hosts[q]) st = LES_BAD_ARG;
+        if (in_slots[q] < 0 || in_slots[q] >= LES_NSLOTS || !in_hosts[q]) return LES_BAD_ARG;
     const size_t bytes = sizeof(double) * (size_t)c->g.n;
     for (int q = 0; q < n_in && !st; ++q)
         st = check_cuda(c, cudaMemcpyAsync(c->slot[in_slots[q]], in_hosts[q], bytes, cudaMemcpyHostToDevice, c->stream),
