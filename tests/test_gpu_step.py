@@ -317,6 +317,30 @@ def test_step_io_matches_separate_calls(graph, precision):
             c.close()
 
 
+def test_step_io_rejects_bad_arguments_before_copying():
+    """les_step_io checks its arguments before it copies anything: a bad
+    solver, slot or null host pointer returns LES_BAD_ARG with the context's
+    fields untouched."""
+    shape = (24, 12, 12)
+    n = int(np.prod(shape))
+    h = 1.0 / 32
+    with G.Context(G.Mesh(*shape, h, h, h)) as c:
+        c.upload_mask(np.zeros(n, np.uint8))
+        c.build_stencil()
+        u0 = np.linspace(0.0, 1.0, n)
+        c.upload("u", u0)
+        junk = np.full(n, 7.0)
+        bad = G.step_params(nu=les_cases.NU, rho=les_cases.RHO, cs=les_cases.CS, solver=9)
+        with pytest.raises(G.LesError):
+            c.step_io(bad, {"u": junk.ctypes.data}, {})
+        good = G.step_params(nu=les_cases.NU, rho=les_cases.RHO, cs=les_cases.CS, solver=G.SOLVER_JACOBI)
+        with pytest.raises(G.LesError):
+            c.step_io(good, {"u": junk.ctypes.data, 99: junk.ctypes.data}, {})
+        with pytest.raises(G.LesError):
+            c.step_io(good, {"u": junk.ctypes.data, "v": 0}, {})
+        assert same(c.download("u"), u0)
+
+
 def test_step_io_gs_sor_and_partial_outputs():
     """les_step_io with the GS-SOR solver (nothing downloads early) and with a
     subset of the fields in and out: the same fields as separate calls."""
