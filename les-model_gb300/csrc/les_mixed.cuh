@@ -168,9 +168,10 @@ les_status inner_solve_fused(les_ctx* c, const les_pcg_opts* o, ViewF A, SolverS
 // condition kernel and the body's relaunch), each iteration that starts
 // after convergence a few us of early exits.  Measured, 20 steps of
 // 256x128x128: 1 pair 140.4, 2 pairs 144.0, 3 pairs 145.5, 4 pairs 146.1
-// Mcell-steps/s; 512x256x256 unchanged.
+// Mcell-steps/s; 512x256x256 unchanged.  With the later, faster passes:
+// 4 pairs 170.0, 6 pairs 170.7, 8 pairs 171.1.
 #ifndef INNER_BODY_PAIRS
-#define INNER_BODY_PAIRS 4
+#define INNER_BODY_PAIRS 8
 #endif
 
 struct BatchCase {
