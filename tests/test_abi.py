@@ -54,3 +54,46 @@ def test_no_cpu_fallback_without_gpu():
     assert lib.les_create(C.byref(m), 0, C.byref(h)) == G.NO_DEVICE
     with pytest.raises(G.LesError):
         G.Context(m)
+
+
+def _header_enums():
+    """name -> value of every enumerator in include/les_gb300.h (implicit
+    values counted from the previous one)."""
+    import re
+    src = open(os.path.join(os.path.dirname(G.PKG), "include", "les_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    out = {}
+    for body in re.findall(r"typedef\s+enum\s+\w*\s*\{(.*?)\}", src, flags=re.S):
+        nxt = 0
+        for item in body.split(","):
+            item = item.strip()
+            if not item:
+                continue
+            m = re.match(r"(LES_\w+)\s*(?:=\s*(-?\d+))?$", item)
+            assert m, item
+            val = int(m.group(2)) if m.group(2) is not None else nxt
+            out[m.group(1)] = val
+            nxt = val + 1
+    return out
+
+
+def test_binding_constants_match_the_header():
+    """The ctypes binding's status, slot, solver, preconditioner, precision
+    and option numbers are the header's (no drift when an enumerator is
+    added)."""
+    e = _header_enums()
+    pairs = {"OK": "LES_OK", "NOT_CONVERGED": "LES_NOT_CONVERGED", "NONFINITE": "LES_NONFINITE",
+             "BAD_ARG": "LES_BAD_ARG", "CUDA_ERROR": "LES_CUDA_ERROR", "NO_DEVICE": "LES_NO_DEVICE",
+             "TIMEOUT": "LES_TIMEOUT",
+             "U": "LES_U", "V": "LES_V", "W": "LES_W", "U_NEW": "LES_U_NEW", "V_NEW": "LES_V_NEW",
+             "W_NEW": "LES_W_NEW", "P": "LES_P", "P_RHS": "LES_P_RHS", "NU_T": "LES_NU_T", "B": "LES_B",
+             "SOLVER_PCG": "LES_SOLVER_PCG", "SOLVER_JACOBI": "LES_SOLVER_JACOBI", "SOLVER_GS": "LES_SOLVER_GS_SOR",
+             "PC_JACOBI": "LES_PC_JACOBI", "PC_IC": "LES_PC_IC", "PC_CHEBYSHEV": "LES_PC_CHEBYSHEV",
+             "PC_IC_A": "LES_PC_IC_A", "FP64": "LES_FP64", "MIXED": "LES_MIXED"}
+    for opt in [k for k in e if k.startswith("LES_OPT_")]:
+        pairs[opt[len("LES_"):]] = opt
+    missing = [py for py, c in pairs.items() if c not in e]
+    assert not missing, missing
+    wrong = {py: (getattr(G, py, None), e[c]) for py, c in pairs.items() if getattr(G, py, None) != e[c]}
+    assert not wrong, wrong
+    assert e["LES_NSLOTS"] == 10
